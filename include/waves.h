@@ -1,0 +1,229 @@
+/*
+ * waves.h — C ABI of the GB300-native waves solver step.
+ *
+ * One handle owns one simulation on one CUDA device: both physical banks (F, u, v, w, p), the
+ * geometry/coefficient work arrays, the multigrid hierarchy, the device control block and its
+ * CUDA stream.  No pointer to device memory escapes; every exchange with the caller goes through
+ * host buffers that the caller owns.
+ *
+ * Each entry point names the GDScript interface it replaces in neuron-forest/waves:
+ *   water/pressure_gpu.gd   — _init/start (:40-47), request (:48-49), request_time (:52-54),
+ *                             close (:55-59), _stats (:133-137), planes/kinds textures (:4-5)
+ *   water/coupled_gpu.gd    — step recorder _record_commands (:38-56), _stats (:58-65)
+ *   water/coastal_gpu.gd    — coastal forcing layer (:1-38)
+ *   water/pressure_multigrid.gd, water/pressure_hierarchy_state.gd — preconditioner (:33-198, :13-41)
+ *   water/lab_runner.gd:19-26 — the beach settings dictionary (waves_config_beach)
+ *
+ * Threading: a handle is used by one thread at a time, except waves_request_steps /
+ * waves_request_time, which may be called from any thread (the quota is an atomic).
+ * Errors never abort the process: every call returns a waves_status; solver failures are the
+ * reference's codes in waves_stats_t.failure.
+ */
+#ifndef WAVES_H
+#define WAVES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WAVES_ABI_VERSION 1
+
+/* Number of doubles in the device control block (reference c[], 96 floats, coastal_gpu.gd:8,
+ * widened to FP64 and extended with build-only slots from index 96). */
+#define WAVES_CONTROL_SIZE 128
+
+typedef enum waves_status {
+  WAVES_OK = 0,
+  WAVES_INVALID_ARG = 1,
+  WAVES_CUDA_ERROR = 2,
+  WAVES_NO_DEVICE = 3,
+  WAVES_SOLVER_FAILED = 4, /* stats.failure != 0 (the reference halts, work_scheduler.gd:44) */
+  WAVES_NOT_READY = 5,
+  WAVES_OUT_OF_MEMORY = 6
+} waves_status;
+
+/* Settings dictionary + push-constant fields of the reference (pressure_gpu.gd:67-68,
+ * coupled_gpu.gd:16-22, coastal_gpu.gd:21-25) plus the multigrid options set in
+ * pressure_gpu.gd:42-43.  Floats are what the reference packs as FP32 push constants. */
+typedef struct waves_config {
+  int32_t n[3];              /* cells nx, ny, nz                           settings "n" */
+  float spacing[3];          /* cell size hx, hy, hz (m)                   settings "spacing" */
+  float origin[3];           /* lower corner of cell (0,0,0) (m)           settings "origin" */
+  float eta;                 /* still-water level (m)                      settings "eta" */
+  float dt;                  /* maximum time step (s), default 1/120       settings "dt" */
+  int32_t periodic_x;        /* x periodic                                 settings "periodic_x" */
+  float slope;               /* bed slope denominator, 0 = flat floor      settings "slope" */
+  float corrugation;         /* cosine surface amplitude (m)               settings "corrugation" */
+  float corrugation_phase;   /* phase added to the cosine (rad); 0 in the reference */
+  int32_t shape;             /* initial fixture 0..7                       settings "shape" */
+  float gravity;             /* gravity multiplier                         settings "gravity" */
+  int32_t max_face_cfl;      /* CFL as max over axes (else sum)            settings "max_face_cfl" */
+  int32_t history_capacity;  /* rows of per-step history                   settings "history_capacity" */
+  float wave[4];             /* amplitude, k, omega, depth                 settings "wave" */
+  float pressure_tolerance;  /* CG relative tolerance, default 1e-4        settings "pressure_tolerance" */
+  int32_t linear_air;        /* linear air extension                       settings "linear_air" */
+  int32_t stokes_second;     /* second-order Stokes target                 settings "stokes_second" */
+  int32_t height_normals;    /* height-function normals (flag bit 0)       settings "height_normals" */
+  int32_t active_advection;  /* valid-band advection (flag bit 1)          settings "active_advection" */
+  int32_t transport_cache;   /* cached MacCormack traces (flag bit 2)      settings "transport_cache" */
+  int32_t transport_interior;/* interior sampling fast path (flag bit 3)   settings "transport_interior" */
+  int32_t coastal;           /* 1: coastal_gpu.gd (offshore forcing, ocean ghost at x<0);
+                                0: coupled_gpu.gd wall variant (the #ifndef COASTAL branches) */
+  float zone_length;         /* offshore relaxation zone (m)               settings "zone_length" */
+  float damping_rate;        /* maximum relaxation rate (1/s)              settings "damping_rate" */
+  float ramp_periods;        /* forcing ramp in wave periods               settings "ramp_periods" */
+  float right_absorption;    /* right absorber scale (shape 6)             settings "right_absorption" */
+  int32_t mg_smoother;       /* 0 jacobi, 1 chebyshev                      config "mg_smoother" */
+  int32_t mg_smoothing;      /* sweeps per smoothing call (1..8)           config "mg_smoothing" */
+  int32_t mg_maintenance;    /* 0 rebuild, 1 structure, 2 lagged           config "mg_maintenance" */
+  int32_t mg_lag;            /* lag in trials for "lagged"                 config "mg_lag" */
+  int32_t mg_aggregate_from; /* first level using aggregation transfers    config "mg_aggregate_from" */
+  int32_t iterations_per_batch; /* CG iterations per scheduler batch (8)   coupled_gpu.gd:14 */
+  float cfl;                 /* CFL limit; the reference hard-codes 0.45 (coupled_motion.glslinc:364) */
+  /* Additions with no reference counterpart. */
+  int32_t mg_precision;      /* 32: FP32 multigrid; 16: BF16 storage and smoothing, FP32 accumulation */
+  int32_t warm_start;        /* 0: previous accepted pressure (reference); 1: learned network */
+  int32_t device;            /* CUDA device ordinal */
+} waves_config;
+
+/* Telemetry of pressure_gpu.gd:135, coupled_gpu.gd:64 and coastal_gpu.gd:37.
+ * Recoverable trial failures (codes 10-12, 20 with retries left) read 0 in `failure`, as in
+ * coupled_gpu.gd:61-62; `trial_failure` keeps the raw code. */
+typedef struct waves_stats_t {
+  int32_t accepted_index;        /* c0 */
+  double accepted_time;          /* c1 */
+  int64_t accepted_steps;        /* c2 */
+  int64_t rejections;            /* c3 */
+  int32_t pending;               /* c4 */
+  int32_t converged;             /* c6 */
+  int32_t failure;               /* c7 masked */
+  int32_t trial_failure;         /* c7 */
+  int64_t iterations;            /* c8 */
+  double relative_residual;      /* c13 */
+  double max_dt_divergence;      /* c14 */
+  double max_face_speed;         /* c15 */
+  double hydrostatic_error_pa;   /* c16 */
+  double volume_m3;              /* c17 */
+  int64_t total_iterations;      /* c18 */
+  double dt;                     /* c20 */
+  double signed_roundoff_m3;     /* c24 */
+  double absolute_roundoff_m3;   /* c25 */
+  double initial_volume_m3;      /* c26 */
+  double max_CFL;                /* c27 */
+  double mass_defect_m3;         /* c28 */
+  int32_t retry_count;           /* c29 */
+  int64_t trial_count;           /* c32 */
+  int32_t last_rejection_code;   /* c33 */
+  double last_rejected_dt;       /* c34 */
+  double compression_volume_m3;  /* c35 */
+  int64_t compression_coverage_errors; /* c36 */
+  double step_start_volume_m3;   /* c37 */
+  double raw_compression_volume_m3; /* c38 */
+  double tentative_outflow_m3;   /* c39 */
+  double boundary_outflow_m3;    /* c40 */
+  int32_t pressure_defect_corrections; /* c58 */
+  double true_relative_residual; /* c60 */
+  double rhs_integrated_divergence_l2;      /* c62 */
+  double residual_integrated_divergence_l2; /* c63 */
+  double forcing_volume_m3;      /* c72 */
+  double ocean_inflow_m3;        /* c73 */
+  double ocean_outflow_m3;       /* c74 */
+  double forcing_momentum[3];    /* c75..77 */
+  double gauges_m[8];            /* c80..87 */
+  double forcing_min_F;          /* c88 */
+  double forcing_max_F;          /* c89 */
+  double conservation_residual_m3; /* FP64 ledger identity (build addition), c100 */
+  int64_t mg_builds;             /* hierarchy numeric rebuilds (pressure_hierarchy_state.glsl state[11]) */
+  int64_t mg_structure_builds;   /* structural rebuilds (state[12]) */
+  int32_t mg_levels;             /* levels in the hierarchy (pressure_multigrid.gd:40-59) */
+  int64_t warm_start_used;       /* trials whose initial pressure came from the learned network */
+} waves_stats_t;
+
+typedef struct waves_handle waves_handle;
+
+/* Defaults of pressure_gpu.gd:40-44, coupled_gpu.gd:7-15, coastal_gpu.gd:5-8, the 64x48x16
+ * flat-floor tank otherwise. */
+void waves_config_default(waves_config* cfg);
+/* lab_runner.gd:19-26: the 310x48x80 beach (dispersion solved by the same 80-step bisection). */
+void waves_config_beach(waves_config* cfg);
+/* 64x48x16 wall-variant sloshing tank, surface 0.45 + 0.05 sin(2 pi x / 1.6) m. */
+void waves_config_tank(waves_config* cfg);
+/* k solving omega^2 = g k tanh(k h) by 80 bisection steps on [0, 100] (lab_runner.gd:19-25). */
+double waves_dispersion_k(double period_s, double depth_m);
+
+/* pressure_gpu.gd _init + start + _initialize: allocates everything on cfg->device, builds the
+ * multigrid level plan, runs the initial commands (coupled_gpu.gd:34-37, coastal_gpu.gd:26-27).
+ * On failure *out is NULL and the reference's host code (97 MG, 98/99 device) is in the status. */
+waves_status waves_create(const waves_config* cfg, waves_handle** out);
+/* pressure_gpu.gd close()/_free(): releases all device memory in reverse order of creation. */
+void waves_destroy(waves_handle* h);
+
+/* Quota, pressure_gpu.gd:48-54: a nonnegative value is an accepted-step count, request_time sets
+ * an absolute accepted-time deadline.  Re-issuing is idempotent; only acceptance advances time. */
+waves_status waves_request_steps(waves_handle* h, int64_t steps);
+waves_status waves_request_time(waves_handle* h, double seconds);
+
+/* Enqueue up to `max_trials` solver trials (one trial = CFL, VOF, MacCormack, forcing, MG build,
+ * PCG to convergence incl. defect corrections, acceptance) on the handle's stream.  No host
+ * synchronisation inside; a trial that finds the quota met or the solver failed does nothing. */
+waves_status waves_advance(waves_handle* h, int32_t max_trials);
+/* Advance until the quota is met or the solver fails (synchronises once per `trials_per_sync`). */
+waves_status waves_run(waves_handle* h, int32_t trials_per_sync);
+/* Wait for the handle's stream. */
+waves_status waves_synchronize(waves_handle* h);
+
+/* Telemetry snapshot (synchronises with the stream). */
+waves_status waves_stats(waves_handle* h, waves_stats_t* out);
+/* Raw control block, WAVES_CONTROL_SIZE doubles in the reference's index map. */
+waves_status waves_control(waves_handle* h, double* c, int32_t count);
+/* Overwrite the control block (test and checkpoint use; count <= WAVES_CONTROL_SIZE). */
+waves_status waves_set_control(waves_handle* h, const double* c, int32_t count);
+/* Host-side fault injection (the reference's op 15, pressure_pass.glslinc:138): sets the
+ * inject-rejection flag c19 so that the next acceptance test rejects the trial with code 4. */
+waves_status waves_inject_rejection(waves_handle* h);
+
+/* Accepted-surface export (pressure_pass.glslinc:127-130, op 19): planes[4N] = (normal, alpha)
+ * per cell and kinds[N] = 0 air, 1 liquid, 2 mixed, x-fastest.  Host buffers. */
+waves_status waves_export_surface(waves_handle* h, float* planes, float* kinds);
+
+/* Bank access.  bank = 0/1 physical bank, -1 the accepted bank.  A bank is
+ * [F: N][u: (nx+1) ny nz][v: nx (ny+1) nz][w: nx ny (nz+1)][p: N] floats, x-fastest. */
+size_t waves_bank_floats(const waves_handle* h);
+waves_status waves_get_bank(waves_handle* h, int32_t bank, float* out);
+waves_status waves_set_bank(waves_handle* h, int32_t bank, const float* in);
+/* Signed distance phi and kind (-1 solid, 0 air, 1 wet) of the last geometry pass, N each. */
+waves_status waves_get_geometry(waves_handle* h, float* phi, float* kind);
+/* Banked pressure masks pmask[2N] and face valid bands vband[2 faces] (coupled_motion.glslinc:
+ * 323-337), bank 0 first; values 0/1. */
+waves_status waves_get_masks(waves_handle* h, float* pmask, float* vband);
+waves_status waves_set_masks(waves_handle* h, const float* pmask, const float* vband);
+
+/* Checkpoint of both banks, the control block, the pressure masks and valid bands and the
+ * hierarchy snapshot: waves_save with buffer NULL returns the size in *bytes. */
+waves_status waves_save(waves_handle* h, void* buffer, size_t* bytes);
+waves_status waves_load(waves_handle* h, const void* buffer, size_t bytes);
+
+/* Learned warm start (no reference counterpart): 4 layers of 3x3x3 convolutions,
+ * channels 3 -> 16 -> 16 -> 16 -> 1, BF16 weights (raw uint16 bit patterns), FP32 biases.
+ * Layout per layer: weights[co][kz][ky][kx][ci].  NULL disables it. */
+#define WAVES_NET_LAYERS 4
+#define WAVES_NET_HIDDEN 16
+typedef struct waves_warm_start_model {
+  const uint16_t* weights[WAVES_NET_LAYERS];
+  const float* bias[WAVES_NET_LAYERS];
+  float input_scale[3];  /* F, b, p_prev multipliers applied before the network */
+  float output_scale;    /* network output multiplier */
+} waves_warm_start_model;
+waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model* model);
+
+/* Last error text of this handle (or of the last failed waves_create when h is NULL). */
+const char* waves_last_error(const waves_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WAVES_H */

@@ -1,0 +1,175 @@
+// TEST INFRASTRUCTURE ONLY — C entry points of the CPU oracle (wo_solver.hpp) for the pytest
+// suite (ctypes) and for bench.py's CPU-baseline leg.  Never linked into the product library.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <memory>
+
+#include "wo_solver.hpp"
+
+namespace {
+struct Box {
+  int precision = 32;
+  std::unique_ptr<wo::Solver<float>> f;
+  std::unique_ptr<wo::Solver<double>> d;
+};
+template <class Fn> auto with(void* h, Fn fn) {
+  Box* b = static_cast<Box*>(h);
+  if (b->precision == 64) return fn(*b->d);
+  return fn(*b->f);
+}
+template <class R> void copy_out(const std::vector<R>& v, float* out) {
+  for (size_t i = 0; i < v.size(); i++) out[i] = float(v[i]);
+}
+template <class R> void copy_in(std::vector<R>& v, const float* in) {
+  for (size_t i = 0; i < v.size(); i++) v[i] = R(in[i]);
+}
+}  // namespace
+
+extern "C" {
+
+// precision 32: FP32 decision-parity oracle; 64: FP64 error oracle.  Runs the initial commands.
+void* wo_create(const waves_config* cfg, int precision) {
+  Box* b = new Box;
+  b->precision = precision;
+  if (precision == 64) {
+    b->d.reset(new wo::Solver<double>(*cfg));
+    b->d->initial_commands();
+  } else {
+    b->f.reset(new wo::Solver<float>(*cfg));
+    b->f->initial_commands();
+  }
+  return b;
+}
+void wo_destroy(void* h) { delete static_cast<Box*>(h); }
+void wo_set_quota(void* h, double quota) {
+  with(h, [&](auto& s) { s.quota = quota; return 0; });
+}
+int wo_run(void* h, int max_batches) {
+  return with(h, [&](auto& s) { return s.run(max_batches); });
+}
+void wo_batch(void* h) {
+  with(h, [&](auto& s) { s.batch(); return 0; });
+}
+void wo_get_control(void* h, double* out) {
+  with(h, [&](auto& s) { std::memcpy(out, s.c, sizeof(s.c)); return 0; });
+}
+void wo_set_control(void* h, const double* in) {
+  with(h, [&](auto& s) { std::memcpy(s.c, in, sizeof(s.c)); return 0; });
+}
+size_t wo_bank_floats(void* h) {
+  return with(h, [&](auto& s) { return s.S; });
+}
+void wo_get_bank(void* h, int bank, float* out) {
+  with(h, [&](auto& s) { copy_out(s.bank[bank], out); return 0; });
+}
+void wo_get_bank_d(void* h, int bank, double* out) {
+  with(h, [&](auto& s) {
+    for (size_t i = 0; i < s.S; i++) out[i] = double(s.bank[bank][i]);
+    return 0;
+  });
+}
+void wo_set_bank(void* h, int bank, const float* in) {
+  with(h, [&](auto& s) { copy_in(s.bank[bank], in); return 0; });
+}
+void wo_get_geometry(void* h, float* phi, float* kind) {
+  with(h, [&](auto& s) { copy_out(s.gphi, phi); copy_out(s.gkind, kind); return 0; });
+}
+// Pressure masks and valid bands of both banks: pmask[2N], vband[2 faces].
+void wo_get_masks(void* h, float* pmask, float* vband) {
+  with(h, [&](auto& s) {
+    for (int b = 0; b < 2; b++) {
+      copy_out(s.pmask[b], pmask + b * s.N);
+      copy_out(s.vband[b], vband + b * s.NF);
+    }
+    return 0;
+  });
+}
+void wo_set_masks(void* h, const float* pmask, const float* vband) {
+  with(h, [&](auto& s) {
+    for (int b = 0; b < 2; b++) {
+      copy_in(s.pmask[b], pmask + b * s.N);
+      copy_in(s.vband[b], vband + b * s.NF);
+    }
+    return 0;
+  });
+}
+void wo_get_export(void* h, float* planes, float* kinds) {
+  with(h, [&](auto& s) {
+    for (size_t i = 0; i < s.N; i++) {
+      planes[4 * i] = float(s.exp_plane[i].x);
+      planes[4 * i + 1] = float(s.exp_plane[i].y);
+      planes[4 * i + 2] = float(s.exp_plane[i].z);
+      planes[4 * i + 3] = float(s.exp_plane[i].w);
+      kinds[i] = float(s.exp_kind[i]);
+    }
+    return 0;
+  });
+}
+void wo_get_probes(void* h, float* out32) {
+  with(h, [&](auto& s) {
+    for (int i = 0; i < 8; i++)
+      for (int k = 0; k < 4; k++) out32[4 * i + k] = float(s.probe[i][k]);
+    return 0;
+  });
+}
+int wo_mg_levels(void* h, int* dims, int* stencils) {
+  return with(h, [&](auto& s) {
+    int L = s.L();
+    for (int l = 0; l < L; l++) {
+      for (int a = 0; a < 3; a++) dims[3 * l + a] = s.mg.levels[l].n[a];
+      stencils[l] = int(s.mg.levels[l].stencil.size());
+    }
+    return L;
+  });
+}
+// Stencil offsets of level l (3 ints each).
+int wo_mg_stencil(void* h, int l, int* offsets) {
+  return with(h, [&](auto& s) {
+    const auto& st = s.mg.levels[l].stencil;
+    for (size_t k = 0; k < st.size(); k++)
+      for (int a = 0; a < 3; a++) offsets[3 * k + a] = st[k][a];
+    return int(st.size());
+  });
+}
+// Multigrid audit state header (first 32 words).
+void wo_mg_state(void* h, uint32_t* out32) {
+  with(h, [&](auto& s) {
+    for (int k = 0; k < 32; k++) out32[k] = s.mg.state[k];
+    return 0;
+  });
+}
+// Step history rows (4 per trial) and coastal history rows (5 per step), vec4 each.
+void wo_get_history(void* h, float* hist, float* chist) {
+  with(h, [&](auto& s) {
+    for (size_t i = 0; i < s.history.size(); i++)
+      for (int k = 0; k < 4; k++) hist[4 * i + k] = float(s.history[i][k]);
+    for (size_t i = 0; i < s.chistory.size(); i++)
+      for (int k = 0; k < 4; k++) chist[4 * i + k] = float(s.chistory[i][k]);
+    return 0;
+  });
+}
+
+// Closed-form PLIC functions in FP32 (plic_math.glslinc:3-37).
+float wo_cube_volume(float nx, float ny, float nz, float alpha) {
+  return wo::Solver<float>::cube_volume(wo::V3<float>(nx, ny, nz), alpha);
+}
+float wo_inverse_volume(float nx, float ny, float nz, float f) {
+  return wo::Solver<float>::inverse_volume(wo::V3<float>(nx, ny, nz), f);
+}
+double wo_cube_volume_d(double nx, double ny, double nz, double alpha) {
+  return wo::Solver<double>::cube_volume(wo::V3<double>(nx, ny, nz), alpha);
+}
+double wo_inverse_volume_d(double nx, double ny, double nz, double f) {
+  return wo::Solver<double>::inverse_volume(wo::V3<double>(nx, ny, nz), f);
+}
+
+// Seconds of wall time for `batches` batches (CPU-baseline timing).
+double wo_time_batches(void* h, int batches) {
+  auto t0 = std::chrono::steady_clock::now();
+  with(h, [&](auto& s) { return s.run(batches); });
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"
