@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
+#include <string>
 
 #include "wo_solver.hpp"
 
@@ -162,6 +163,51 @@ double wo_cube_volume_d(double nx, double ny, double nz, double alpha) {
 }
 double wo_inverse_volume_d(double nx, double ny, double nz, double f) {
   return wo::Solver<double>::inverse_volume(wo::V3<double>(nx, ny, nz), f);
+}
+
+// Run one phase of a batch, in the phase numbering of include/waves_debug.h.
+void wo_phase(void* h, int phase) {
+  with(h, [&](auto& s) {
+    switch (phase) {
+      case 0: s.op43(); s.op1(); break;
+      case 1: s.op20_21(); s.op45_46(); s.op22(); break;
+      case 2: s.op23(); s.op24(); s.op55_56(); s.op25_26(); break;
+      case 3: s.op27_28(27); s.op27_28(28); break;
+      case 4: if (s.coastal) { s.op80_81(); s.op82(); s.op83_84(); s.op87_88(); } break;
+      case 5: s.op17(); s.op18(); s.op16(); break;
+      case 6: s.op2(); s.op47(); break;
+      case 7: s.mg_build(); break;
+      case 8: s.op63(); s.op64(); s.op3(); s.mg_cycle(0); s.op4(); break;
+      case 9: s.op5(); s.op6_7(); s.op8(); s.mg_cycle(1); s.op9(); s.op10(); break;
+      case 10: s.op11(); s.op65(); s.op47(); s.op30(); s.op31_33(31); s.op31_33(32); s.op31_33(33); s.op34();
+               s.op47(); s.op48_49(false); s.op35_36(); s.op62_66(); s.op12_13(); break;
+      case 11: s.op44(); if (s.coastal) { s.op85(); s.op89(); } break;
+    }
+    return 0;
+  });
+}
+// Scratch arrays by name (float copies): "fwd", "plane" (4N), "coef" (6N), "diag", "r", "z", "d", "q", "b",
+// "tcache" (6 faces), "mF", "mci", "src1" (as float).
+int wo_read(void* h, const char* name, float* out) {
+  return with(h, [&](auto& s) {
+    std::string n(name);
+    if (n == "fwd") copy_out(s.fwd, out);
+    else if (n == "mF") copy_out(s.mF, out);
+    else if (n == "mci") copy_out(s.mci, out);
+    else if (n == "plane") { for (size_t i = 0; i < s.N; i++) for (int k = 0; k < 4; k++) out[4 * i + k] = float(s.plane[i][k]); }
+    else if (n == "coef") { for (size_t i = 0; i < 6 * s.N; i++) out[i] = float(s.work[6 * s.N + i]); }
+    else if (n == "diag") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[12 * s.N + i]); }
+    else if (n == "r") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[i]); }
+    else if (n == "z") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[s.N + i]); }
+    else if (n == "d") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[2 * s.N + i]); }
+    else if (n == "q") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[3 * s.N + i]); }
+    else if (n == "b") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[5 * s.N + i]); }
+    else if (n == "pbase") { for (size_t i = 0; i < s.N; i++) out[i] = float(s.work[13 * s.N + i]); }
+    else if (n == "tcache") { for (int k = 0; k < 6; k++) copy_out(s.tcache[k], out + k * s.NF); }
+    else if (n == "src1") { for (size_t i = 0; i < s.NF; i++) out[i] = float(s.src[1][i]); }
+    else return 0;
+    return 1;
+  });
 }
 
 // Seconds of wall time for `batches` batches (CPU-baseline timing).

@@ -1,0 +1,186 @@
+"""GB300-native waves solver step.
+
+`load()` returns the in-tree C-ABI library (libwaves_gb300.so, built by waves_gb300/build.py);
+`WavesSolver` is a thin Python handle over it, and `CoastalGPU` / `CoupledGPU` mirror the
+GDScript classes of the reference (water/coastal_gpu.gd, water/coupled_gpu.gd,
+water/pressure_gpu.gd) with the same method names and quota semantics.
+
+There is no CPU fallback: every call goes through the CUDA library, and constructing a solver
+without it (or without a CUDA device) raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import WavesConfig, WavesStats, WAVES_CONTROL_SIZE
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libwaves_gb300.so")
+_lib = None
+
+
+def load(build_if_missing=False):
+    """The product library, loaded once.  Raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(f"waves_gb300 CUDA library missing: {LIB_PATH} (run waves_gb300/build.py)")
+        from .build import build
+        build()
+    _lib = abi.declare(C.CDLL(LIB_PATH))
+    return _lib
+
+
+class WavesError(RuntimeError):
+    pass
+
+
+def _check(lib, status, h=None):
+    if status != 0:
+        msg = lib.waves_last_error(h)
+        raise WavesError(f"{abi.STATUS.get(status, status)}: {msg.decode() if msg else ''}")
+
+
+def config(preset="default", **overrides):
+    """A WavesConfig from a preset ('default', 'beach', 'tank') with field overrides."""
+    lib = load()
+    cfg = WavesConfig()
+    {"default": lib.waves_config_default, "beach": lib.waves_config_beach, "tank": lib.waves_config_tank}[preset](C.byref(cfg))
+    for k, v in overrides.items():
+        field = getattr(cfg, k)
+        if hasattr(field, "__len__"):
+            for i, x in enumerate(v):
+                field[i] = x
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+def dispersion_k(period_s, depth_m):
+    return load().waves_dispersion_k(period_s, depth_m)
+
+
+class WavesSolver:
+    """One simulation on one CUDA device (a waves_handle)."""
+
+    def __init__(self, cfg: WavesConfig):
+        self.lib = load()
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = self.lib.waves_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            msg = self.lib.waves_last_error(None)
+            raise WavesError(f"waves_create: {abi.STATUS.get(st, st)}: {msg.decode() if msg else ''}")
+        self.h = h
+        n = cfg.n
+        self.N = n[0] * n[1] * n[2]
+        self.NU = (n[0] + 1) * n[1] * n[2]
+        self.NV = n[0] * (n[1] + 1) * n[2]
+        self.NW = n[0] * n[1] * (n[2] + 1)
+        self.NF = self.NU + self.NV + self.NW
+        self.S = self.lib.waves_bank_floats(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.waves_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _ck(self, st):
+        _check(self.lib, st, self.h)
+
+    def request_steps(self, steps):
+        self._ck(self.lib.waves_request_steps(self.h, int(steps)))
+
+    def request_time(self, seconds):
+        self._ck(self.lib.waves_request_time(self.h, float(seconds)))
+
+    def advance(self, trials):
+        self._ck(self.lib.waves_advance(self.h, int(trials)))
+
+    def run(self, trials_per_sync=4):
+        st = self.lib.waves_run(self.h, int(trials_per_sync))
+        if st not in (0, 4):
+            self._ck(st)
+        return st
+
+    def synchronize(self):
+        self._ck(self.lib.waves_synchronize(self.h))
+
+    def stats(self):
+        s = WavesStats()
+        self._ck(self.lib.waves_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def control(self):
+        c = (C.c_double * WAVES_CONTROL_SIZE)()
+        self._ck(self.lib.waves_control(self.h, c, WAVES_CONTROL_SIZE))
+        return np.frombuffer(c, dtype=np.float64).copy()
+
+    def set_control(self, c):
+        arr = np.ascontiguousarray(c, dtype=np.float64)
+        self._ck(self.lib.waves_set_control(self.h, arr.ctypes.data_as(C.POINTER(C.c_double)), len(arr)))
+
+    def inject_rejection(self):
+        self._ck(self.lib.waves_inject_rejection(self.h))
+
+    def bank(self, which=-1):
+        out = np.empty(self.S, dtype=np.float32)
+        self._ck(self.lib.waves_get_bank(self.h, which, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_bank(self, which, data):
+        arr = np.ascontiguousarray(data, dtype=np.float32)
+        assert arr.size == self.S
+        self._ck(self.lib.waves_set_bank(self.h, which, arr.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def geometry(self):
+        phi = np.empty(self.N, dtype=np.float32)
+        kind = np.empty(self.N, dtype=np.float32)
+        self._ck(self.lib.waves_get_geometry(self.h, phi.ctypes.data_as(C.POINTER(C.c_float)),
+                                             kind.ctypes.data_as(C.POINTER(C.c_float))))
+        return phi, kind
+
+    def masks(self):
+        pm = np.empty(2 * self.N, dtype=np.float32)
+        vb = np.empty(2 * self.NF, dtype=np.float32)
+        self._ck(self.lib.waves_get_masks(self.h, pm.ctypes.data_as(C.POINTER(C.c_float)),
+                                          vb.ctypes.data_as(C.POINTER(C.c_float))))
+        return pm, vb
+
+    def set_masks(self, pm, vb):
+        pm = np.ascontiguousarray(pm, dtype=np.float32)
+        vb = np.ascontiguousarray(vb, dtype=np.float32)
+        self._ck(self.lib.waves_set_masks(self.h, pm.ctypes.data_as(C.POINTER(C.c_float)),
+                                          vb.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def export_surface(self):
+        planes = np.empty(4 * self.N, dtype=np.float32)
+        kinds = np.empty(self.N, dtype=np.float32)
+        self._ck(self.lib.waves_export_surface(self.h, planes.ctypes.data_as(C.POINTER(C.c_float)),
+                                               kinds.ctypes.data_as(C.POINTER(C.c_float))))
+        return planes.reshape(-1, 4), kinds
+
+    def save(self):
+        n = C.c_size_t(0)
+        self._ck(self.lib.waves_save(self.h, None, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        self._ck(self.lib.waves_save(self.h, buf.ctypes.data_as(C.c_void_p), C.byref(n)))
+        return buf
+
+    def load(self, buf):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self._ck(self.lib.waves_load(self.h, buf.ctypes.data_as(C.c_void_p), buf.size))
+
+    def split_bank(self, b):
+        """F, u, v, w, p views of a bank array (x-fastest flat arrays)."""
+        N, NU, NV, NW = self.N, self.NU, self.NV, self.NW
+        return b[:N], b[N:N + NU], b[N + NU:N + NU + NV], b[N + NU + NV:N + NU + NV + NW], b[N + NU + NV + NW:]
+
+
+from .gd import CoastalGPU, CoupledGPU, PressureGPU  # noqa: E402,F401

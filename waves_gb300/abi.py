@@ -195,6 +195,9 @@ def declare(lib):
         "waves_set_warm_start": (C.c_int, [h, P(WavesWarmStartModel)]),
         "waves_last_error": (C.c_char_p, [h]),
     }
+    sig["waves_debug_phase"] = (C.c_int, [h, C.c_int32])
+    sig["waves_debug_sample"] = (C.c_int, [h, P(C.c_float), C.c_int32, C.c_int32, P(C.c_float)])
+    sig["waves_debug_read"] = (C.c_int, [h, C.c_char_p, C.c_void_p, C.c_size_t])
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res

@@ -1,0 +1,442 @@
+// Device arithmetic of the waves solver step, shared by all kernels.
+//
+// Every function restates the reference shader function named in its comment
+// (neuron-forest/waves water/shaders/compute/*.glslinc) with the same FP32 operations in the same
+// order.  The translation units are compiled with -fmad=false so that no multiply-add is fused
+// unless the reference writes fma(); min/max are plain comparisons; transcendentals are evaluated
+// in double and rounded to float.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "dev.h"
+
+namespace wg {
+
+#define DI __device__ __forceinline__
+
+struct I3 {
+  int x, y, z;
+  DI int& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  DI int operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+DI I3 mk(int x, int y, int z) { I3 q; q.x = x; q.y = y; q.z = z; return q; }
+DI I3 addI(I3 a, I3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+DI I3 subI(I3 a, I3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+DI bool eqI(I3 a, I3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+DI I3 ax(I3 q, int axis, int delta) { q[axis] += delta; return q; }
+
+struct F3 {
+  float x, y, z;
+  DI float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  DI float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+DI F3 mf(float x, float y, float z) { F3 v; v.x = x; v.y = y; v.z = z; return v; }
+DI float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DI float len3(F3 a) { return sqrtf(dot3(a, a)); }
+DI F3 sub3(F3 a, F3 b) { return mf(a.x - b.x, a.y - b.y, a.z - b.z); }
+DI F3 add3(F3 a, F3 b) { return mf(a.x + b.x, a.y + b.y, a.z + b.z); }
+DI F3 mul3(F3 a, F3 b) { return mf(a.x * b.x, a.y * b.y, a.z * b.z); }
+DI F3 div3(F3 a, F3 b) { return mf(a.x / b.x, a.y / b.y, a.z / b.z); }
+DI F3 scl3(F3 a, float s) { return mf(a.x * s, a.y * s, a.z * s); }
+DI F3 abs3(F3 a) { return mf(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+DI float l1(F3 a) { return fabsf(a.x) * 1.f + fabsf(a.y) * 1.f + fabsf(a.z) * 1.f; }
+DI float half_dot(F3 a) { return a.x * .5f + a.y * .5f + a.z * .5f; }
+
+DI float mnf(float a, float b) { return (b < a) ? b : a; }
+DI float mxf(float a, float b) { return (a < b) ? b : a; }
+DI float clampf_(float x, float lo, float hi) { return mnf(mxf(x, lo), hi); }
+DI float fract_(float x) { return x - floorf(x); }
+DI float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+DI float tcos(float x) { return (float)cos((double)x); }
+DI float tsin(float x) { return (float)sin((double)x); }
+DI float ttanh(float x) { return (float)tanh((double)x); }
+DI float tsinh(float x) { return (float)sinh((double)x); }
+DI float tcosh(float x) { return (float)cosh((double)x); }
+DI float texp(float x) { return (float)exp((double)x); }
+DI float tpow4(float x) { double d = (double)x; return (float)(d * d * d * d); }
+// periodic_index.glslinc:3-6
+DI int pidx(int q, int n) { return q >= 0 ? q % n : n - 1 - ((-1 - q) % n); }
+
+// ---------------------------------------------------------------- grid helpers
+struct Grid {
+  const Dev& D;
+  DI explicit Grid(const Dev& d) : D(d) {}
+  DI float h(int a) const { return a == 0 ? D.hx : (a == 1 ? D.hy : D.hz); }
+  DI long long index3(I3 q) const { return (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)D.ny * q.z); }
+  DI I3 coord(long long i) const { return mk(int(i % D.nx), int((i / D.nx) % D.ny), int(i / ((long long)D.nx * D.ny))); }
+  DI I3 wrap_cell(I3 q) const {
+    q.z = pidx(q.z, D.nz);
+    if (D.px) q.x = pidx(q.x, D.nx);
+    return q;
+  }
+  DI bool outside(I3 q) const { return q.x < 0 || q.x >= D.nx || q.y < 0 || q.y >= D.ny; }
+  DI F3 center(I3 q) const {
+    return mf(D.ox + ((float)q.x + 0.5f) * D.hx, D.oy + ((float)q.y + 0.5f) * D.hy, D.oz + ((float)q.z + 0.5f) * D.hz);
+  }
+  // solid (pressure_core.glslinc:87-96), tabulated over (x, y) with a margin
+  DI bool solid_direct(I3 q) const {
+    q = wrap_cell(q);
+    if (q.y < 0 || q.x >= D.nx) return true;
+    if (!D.coastal && q.x < 0) return true;
+    if (q.y >= D.ny) return false;
+    if (D.slope > 0.f) {
+      float x = center(q).x;
+      float bed = -0.45f + mxf(0.f, x - 1.5f) / D.slope;
+      return center(q).y <= bed;
+    }
+    return false;
+  }
+  DI bool solid(I3 q) const {
+    q = wrap_cell(q);
+    int x = q.x + kSolidPad, y = q.y + kSolidPad;
+    if (x >= 0 && y >= 0 && x < D.tab_w && y < D.tab_h) return D.solid_tab[y * D.tab_w + x] != 0;
+    return solid_direct(q);
+  }
+  DI bool wet(I3 q) const {
+    q = wrap_cell(q);
+    return !outside(q) && D.kind[index3(q)] > 0;
+  }
+  // eta (pressure_core.glslinc:73-83)
+  DI float eta(I3 q) const {
+    if (D.shape == 5) {
+      float phase = D.wave[1] * (D.ox + ((float)q.x + .5f) * D.hx);
+      float sigma = ttanh(D.wave[1] * D.wave[3]);
+      float second = D.stokes2 ? D.wave[1] * D.wave[0] * D.wave[0] * (3.f - sigma * sigma) / (4.f * sigma * sigma * sigma) : 0.f;
+      return D.eta0 + D.wave[0] * tcos(phase) + second * tcos(2.f * phase);
+    }
+    return D.eta0 + D.corr * tcos(6.28318530718f * ((float)q.x + 0.5f) / (float)D.nx + D.corr_phase);
+  }
+  DI float phi(I3 q) const {
+    q = wrap_cell(q);
+    return outside(q) ? center(q).y - eta(q) : D.phi[index3(q)];
+  }
+  // face_index (pressure_core.glslinc:129-133), local to the face block (minus U())
+  DI long long face_local(I3 q, int axis) const {
+    if (axis == 2 && q.z == D.nz) q.z = 0;
+    if (axis == 0 && D.px && q.x == D.nx) q.x = 0;
+    if (axis == 0) return (long long)q.x + (long long)(D.nx + 1) * ((long long)q.y + (long long)D.ny * q.z);
+    if (axis == 1) return D.NU + (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)(D.ny + 1) * q.z);
+    return D.NU + D.NV + (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)D.ny * q.z);
+  }
+  DI long long face_index(I3 q, int axis) const { return D.N + face_local(q, axis); }
+  DI void unpack_face(long long f, I3& q, int& axis) const {
+    long long base;
+    int mx_, my_;
+    if (f < D.NU) { axis = 0; base = 0; mx_ = D.nx + 1; my_ = D.ny; }
+    else if (f < D.NU + D.NV) { axis = 1; base = D.NU; mx_ = D.nx; my_ = D.ny + 1; }
+    else { axis = 2; base = D.NU + D.NV; mx_ = D.nx; my_ = D.ny; }
+    long long i = f - base;
+    q = mk(int(i % mx_), int((i / mx_) % my_), int(i / ((long long)mx_ * my_)));
+  }
+  DI bool wall_face(I3 q, int axis) const { return solid(q) || solid(ax(q, axis, -1)); }
+  DI bool face_in_bounds(I3 q, int axis) const {
+    int mx_ = D.nx + (axis == 0), my_ = D.ny + (axis == 1), mz_ = D.nz + (axis == 2);
+    return q.x >= 0 && q.y >= 0 && q.z >= 0 && q.x < mx_ && q.y < my_ && q.z < mz_;
+  }
+  DI I3 wrap_face(I3 q) const {
+    q.z = pidx(q.z, D.nz);
+    if (D.px) q.x = pidx(q.x, D.nx);
+    return q;
+  }
+  DI F3 periodic_delta(I3 a, I3 b) const {
+    F3 d = mf((float)(a.x - b.x), (float)(a.y - b.y), (float)(a.z - b.z));
+    d.z -= roundf(d.z / (float)D.nz) * (float)D.nz;
+    if (D.px) d.x -= roundf(d.x / (float)D.nx) * (float)D.nx;
+    return mf(d.x * D.hx, d.y * D.hy, d.z * D.hz);
+  }
+};
+
+// ---------------------------------------------------------------- plic_math.glslinc
+DI float cube_volume(F3 normal, float alpha) {
+  alpha -= mnf(normal.x, 0.f) + mnf(normal.y, 0.f) + mnf(normal.z, 0.f);
+  F3 v = abs3(normal);
+  float total = v.x + v.y + v.z;
+  if (alpha <= 0.f) return 0.f;
+  if (alpha >= total) return 1.f;
+  float t;
+  if (v.x > v.y) { t = v.x; v.x = v.y; v.y = t; }
+  if (v.y > v.z) { t = v.y; v.y = v.z; v.z = t; }
+  if (v.x > v.y) { t = v.x; v.x = v.y; v.y = t; }
+  bool complement = alpha > 0.5f * total;
+  t = complement ? total - alpha : alpha;
+  float x = v.x, y = v.y, z = v.z, result;
+  if (x < 1e-6f * total) {
+    t -= x * 0.5f;
+    if (y < 1e-6f * total) result = (t - y * 0.5f) / z;
+    else if (t < y) result = t * t / (2.f * y * z);
+    else result = (t - 0.5f * y) / z;
+  } else if (t < x) result = t * t * t / (6.f * x * y * z);
+  else if (t < y) result = (3.f * t * t - 3.f * t * x + x * x) / (6.f * y * z);
+  else if (x + y < z && t >= x + y) result = (t - 0.5f * (x + y)) / z;
+  else {
+    float ty = mxf(t - y, 0.f), tz = mxf(t - z, 0.f);
+    float numerator = x * (3.f * t * t - 3.f * t * x + x * x) - ty * ty * ty - tz * tz * tz;
+    result = numerator / (6.f * x * y * z);
+  }
+  return complement ? 1.0f - result : result;
+}
+DI float inverse_volume(F3 normal, float fraction) {
+  float lo = mnf(normal.x, 0.f) + mnf(normal.y, 0.f) + mnf(normal.z, 0.f);
+  float hi = mxf(normal.x, 0.f) + mxf(normal.y, 0.f) + mxf(normal.z, 0.f);
+  for (int it = 0; it < 25; it++) {
+    float mid = 0.5f * (lo + hi);
+    if (cube_volume(normal, mid) < fraction) lo = mid;
+    else hi = mid;
+  }
+  float alpha = 0.5f * (lo + hi), cen = half_dot(normal);
+  if (fraction == .5f) return cen;
+  if (fraction < .5f) return mnf(alpha, cen);
+  if (alpha <= cen) alpha = cen + 5.96046448e-8f * l1(normal);
+  return alpha;
+}
+
+// ---------------------------------------------------------------- coastal_target.glslinc
+struct Coast {
+  const Dev& D;
+  DI explicit Coast(const Dev& d) : D(d) {}
+  DI static float smooth_ramp(float q) {
+    q = clampf_(q, 0.f, 1.f);
+    return q * q * q * (10.f + q * (-15.f + 6.f * q));
+  }
+  DI float ramped_amplitude(float time) const {
+    return D.wave[0] * smooth_ramp(time * D.wave[2] / (6.28318530718f * D.forcing[3]));
+  }
+  DI void surface(float x, float time, float& s0, float& s1) const {
+    float a = ramped_amplitude(time), k = D.wave[1], w = D.wave[2], hh = D.wave[3];
+    float sigma = ttanh(k * hh), second = k * a * a * (3.f - sigma * sigma) / (4.f * sigma * sigma * sigma);
+    if (!D.stokes2) second = 0.f;
+    float phase = k * (x - D.forcing[0]) - w * time;
+    s0 = a * tcos(phase) + second * tcos(2.f * phase);
+    s1 = -k * a * tsin(phase) - 2.f * k * second * tsin(2.f * phase);
+  }
+  DI F3 velocity(F3 world, float time) const {
+    float a = ramped_amplitude(time), k = D.wave[1], w = D.wave[2], hh = D.wave[3];
+    float s = tsinh(k * hh), phase = k * (world.x - D.forcing[0]) - w * time, y = world.y + hh;
+    float first = a * w / s, second = D.stokes2 ? .75f * a * a * w * k / tpow4(s) : 0.f;
+    return mf(first * tcosh(k * y) * tcos(phase) + second * tcosh(2.f * k * y) * tcos(2.f * phase),
+              first * tsinh(k * y) * tsin(phase) + second * tsinh(2.f * k * y) * tsin(2.f * phase), 0.f);
+  }
+  // single velocity component (avoids the unused transcendentals)
+  DI float velocity_c(F3 world, float time, int axis) const {
+    if (axis == 2) return 0.f;
+    float a = ramped_amplitude(time), k = D.wave[1], w = D.wave[2], hh = D.wave[3];
+    float s = tsinh(k * hh), phase = k * (world.x - D.forcing[0]) - w * time, y = world.y + hh;
+    float first = a * w / s, second = D.stokes2 ? .75f * a * a * w * k / tpow4(s) : 0.f;
+    if (axis == 0) return first * tcosh(k * y) * tcos(phase) + second * tcosh(2.f * k * y) * tcos(2.f * phase);
+    return first * tsinh(k * y) * tsin(phase) + second * tsinh(2.f * k * y) * tsin(2.f * phase);
+  }
+  DI F3 face_position(const Grid& g, I3 q, int axis) const {
+    F3 p = g.center(q);
+    p[axis] -= .5f * g.h(axis);
+    return p;
+  }
+  DI float4 plane(const Grid& g, I3 q, float time) const {
+    float s0, s1;
+    F3 cq = g.center(q);
+    surface(cq.x, time, s0, s1);
+    F3 normal = mf(-s1 * D.hx, D.hy, 0.f);
+    return make_float4(normal.x, normal.y, normal.z, half_dot(normal) + s0 - cq.y);
+  }
+  DI float fraction(const Grid& g, I3 q, float time) const {
+    float4 eq = plane(g, q, time);
+    return clampf_(cube_volume(mf(eq.x, eq.y, eq.z), eq.w), 0.f, 1.f);
+  }
+  DI float rate(float x) const {
+    float left = 1.f - smooth_ramp((x - D.forcing[0]) / D.forcing[1]);
+    float right = D.shape == 6 ? smooth_ramp((x - (D.ox + (float)D.nx * D.hx - D.forcing[1])) / D.forcing[1]) : 0.f;
+    return D.forcing[2] * mxf(left, D.right_abs * right);
+  }
+  DI bool offshore(float x) const { return x < D.forcing[0] + D.forcing[1]; }
+};
+
+// ---------------------------------------------------------------- PLIC reconstruction
+// Normal from a gradient and the plane constant (pressure_geometry.glslinc:58-60,
+// coupled_motion.glslinc:54-55).
+DI float4 plane_from_gradient(const Dev& D, F3 g, float f) {
+  if (len3(g) < 1e-9f) g = mf(0.f, 1.f, 0.f);
+  float L = len3(g);
+  F3 normal = mf(g.x / L * D.hx, g.y / L * D.hy, g.z / L * D.hz);
+  float s = l1(normal);
+  normal = mf(normal.x / s, normal.y / s, normal.z / s);
+  return make_float4(normal.x, normal.y, normal.z, inverse_volume(normal, f));
+}
+
+// Weighted Youngs gradient (pressure_geometry.glslinc:35-53) over a fraction lookup `Fr`.
+template <class Fr> DI F3 interface_gradient(const Grid& g, I3 q, const Fr& fr) {
+  F3 grad = mf(0.f, 0.f, 0.f);
+  for (int axis = 0; axis < 3; axis++) {
+    int b = (axis + 1) % 3, d = (axis + 2) % 3, weights = 0;
+    float acc = 0.f;
+    float hh = g.h(axis);
+    for (int j = -1; j <= 1; j++)
+      for (int k = -1; k <= 1; k++) {
+        I3 middle = q;
+        middle[b] += j;
+        middle[d] += k;
+        if (g.solid(middle)) continue;
+        I3 l = ax(middle, axis, -1), r = ax(middle, axis, 1);
+        bool left = !g.solid(l), right = !g.solid(r);
+        if (!left && !right) continue;
+        float difference;
+        if (left && right) difference = fr(l) - fr(r);
+        else if (left) difference = 2.f * (fr(l) - fr(middle));
+        else difference = 2.f * (fr(middle) - fr(r));
+        int weight = (j == 0 ? 2 : 1) * (k == 0 ? 2 : 1);
+        weights += weight;
+        acc += (float)weight * difference / (32.f * hh);
+      }
+    if (weights > 0) acc *= 16.0f / (float)weights;
+    grad[axis] = acc;
+  }
+  return grad;
+}
+
+// Height-function normal (height_normal.glslinc:6-34), flag bit 0.
+template <class Fr> DI F3 height_normal(const Grid& g, I3 q, F3 youngs, const Fr& fr) {
+  F3 sp = mf(g.D.hx, g.D.hy, g.D.hz);
+  F3 scaled = mul3(abs3(youngs), sp);
+  int axis = scaled.x > scaled.y ? 0 : 1;
+  if (scaled.z > scaled[axis]) axis = 2;
+  if (scaled[axis] < 1e-12f) return youngs;
+  int b = (axis + 1) % 3, d = (axis + 2) % 3;
+  float orientation = sgnf(youngs[axis]);
+  float heights[5];
+  for (int column = 0; column < 5; column++) {
+    I3 base = q;
+    if (column == 1) base[b]--;
+    if (column == 2) base[b]++;
+    if (column == 3) base[d]--;
+    if (column == 4) base[d]++;
+    float sum = 0.f, previous = orientation > 0.f ? 1.f : 0.f;
+    for (int t = -4; t <= 4; t++) {
+      I3 cell = ax(base, axis, t);
+      I3 w = g.wrap_cell(cell);
+      if (g.outside(w) || g.solid(w)) return youngs;
+      float f = fr(cell);
+      if (isnan(f) || isinf(f) || f < 0.f || f > 1.f) return youngs;
+      if (orientation * (f - previous) > 2e-6f) return youngs;
+      if (t == -4 && f != (orientation > 0.f ? 1.f : 0.f)) return youngs;
+      if (t == 4 && f != (orientation > 0.f ? 0.f : 1.f)) return youngs;
+      sum += f;
+      previous = f;
+    }
+    heights[column] = sum * sp[axis];
+  }
+  F3 result = mf(0.f, 0.f, 0.f);
+  result[axis] = orientation;
+  result[b] = -(heights[2] - heights[1]) / (2.f * sp[b]);
+  result[d] = -(heights[4] - heights[3]) / (2.f * sp[d]);
+  return result;
+}
+
+// ---------------------------------------------------------------- deterministic reductions
+// Block-wide reduction in a fixed tree; result valid in thread 0.
+template <int NT, class T, class Op> DI T block_reduce(T v, Op op, T* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_down_sync(0xffffffffu, v, o));
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    v = sh[0];
+    for (int w = 1; w < NT / 32; w++) v = op(v, sh[w]);
+  }
+  __syncthreads();
+  return v;
+}
+struct AddD { DI double operator()(double a, double b) const { return a + b; } };
+struct MaxD { DI double operator()(double a, double b) const { return a < b ? b : a; } };
+struct MinF { DI float operator()(float a, float b) const { return (b < a) ? b : a; } };
+struct MaxF { DI float operator()(float a, float b) const { return (a < b) ? b : a; } };
+
+// Write `K` per-block partials (double), then let the last block to finish reduce all partials
+// in a fixed order.  Returns true in every thread of the last block, with the totals in `out`.
+// `ops[k]` selects 0 = sum, 1 = max for each component.
+template <int NT, int K>
+DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (&ops)[K], double (&out)[K]) {
+  __shared__ double sh[32];
+  __shared__ bool am_last;
+  const int nb = gridDim.x;
+  double* part = D.part;
+  for (int k = 0; k < K; k++) {
+    double r = ops[k] == 0 ? block_reduce<NT>(vals[k], AddD(), sh) : block_reduce<NT>(vals[k], MaxD(), sh);
+    if (threadIdx.x == 0) part[(size_t)k * nb + blockIdx.x] = r;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int prev = atomicAdd(&D.count[site], 1u);
+    am_last = (prev == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  for (int k = 0; k < K; k++) {
+    double acc = ops[k] == 0 ? 0.0 : -1e300;
+    for (int b = threadIdx.x; b < nb; b += NT) {
+      double p = __ldcg(&part[(size_t)k * nb + b]);
+      acc = ops[k] == 0 ? acc + p : (acc < p ? p : acc);
+    }
+    out[k] = ops[k] == 0 ? block_reduce<NT>(acc, AddD(), sh) : block_reduce<NT>(acc, MaxD(), sh);
+  }
+  if (threadIdx.x == 0) D.count[site] = 0;
+  return true;
+}
+
+
+// ---------------------------------------------------------------- PCG control (pressure_core.glslinc:156-179)
+DI bool solving(const Dev& D) { return D.c[4] > 0.5 && D.c[6] < 0.5 && D.c[7] < 0.5; }
+DI bool pressure_setup(const Dev& D) { return D.c[5] > .5 || D.c[57] == 2; }
+
+// pressure_norm_converged / residual_converged (pressure_core.glslinc:173-178)
+DI double scaled_norm(const Dev& D, double sq) {
+  double d = D.c[20];
+  return d * d / 1000 * sqrt(sq > 0 ? sq : 0.0);
+}
+DI bool norm_converged(const Dev& D, double res2, double rhs2) {
+  double t = (double)D.tol;
+  return res2 <= t * t * rhs2 || (scaled_norm(D, rhs2) <= 1e-5 && scaled_norm(D, res2) <= 1e-8);
+}
+DI bool residual_converged(const Dev& D, const double* s, double rhs2) {
+  double d = D.c[20];
+  return norm_converged(D, s[1], rhs2) && d * d / 1000 * s[3] < 5e-5;
+}
+
+// op 4 finalisation (pressure_iterations.glslinc:332-337)
+DI void finalize_op4(const Dev& D, const double* s) {
+  double* c = D.c;
+  c[9] = s[0];
+  c[10] = s[2];
+  c[13] = sqrt(s[1] / (s[2] > 1e-30 ? s[2] : 1e-30));
+  if (residual_converged(D, s, s[2])) c[6] = 1;
+  if (c[58] == 0) c[59] = s[2];
+  c[57] = 0;
+}
+// op 9 finalisation (pressure_iterations.glslinc:349)
+DI void finalize_op9(const Dev& D, const double* s) {
+  double* c = D.c;
+  c[12] = s[0] / (c[9] > 1e-30 ? c[9] : 1e-30);
+  c[9] = s[0];
+  c[8] += 1;
+  c[18] += 1;
+  c[13] = sqrt(s[1] / (c[10] > 1e-30 ? c[10] : 1e-30));
+  if (isnan(c[13]) || isinf(c[13])) c[7] = 2;
+  else if (residual_converged(D, s, c[10])) c[6] = 1;
+  else if (c[8] > 4096) c[7] = 3;
+}
+
+
+// Multigrid storage: FP32 or BF16 values with FP32 arithmetic.
+template <class T> DI T st_val(float x);
+template <> DI float st_val<float>(float x) { return x; }
+template <> DI __nv_bfloat16 st_val<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+DI float ld_val(float x) { return x; }
+DI float ld_val(__nv_bfloat16 x) { return __bfloat162float(x); }
+
+// Read the accepted/candidate bank pointers.
+DI float* bank_ptr(const Dev& D, int b) { return b == 0 ? D.bank0 : D.bank1; }
+DI int acc_bank(const Dev& D) { return (int)D.c[0]; }
+
+}  // namespace wg

@@ -1,0 +1,132 @@
+// Device-side parameter block of one simulation: sizes, push-constant values and raw device
+// pointers.  Passed by value to every kernel (a few hundred bytes of kernel parameters).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace wg {
+
+constexpr int kMaxLevels = 12;
+constexpr int kMaxStencil = 125;
+constexpr int kSolidPad = 16;  // margin of the tabulated solid() lookup
+
+// Indices into the double control block beyond the reference's 96 entries.
+enum CtrlExtra {
+  kSweepRound = 96,     // staged rounding ledger of the three sweeps (FP64)
+  kSweepComp = 97,      // staged compression ledger (FP64)
+  kRoundCommit = 98,    // committed rounding ledger
+  kCompCommit = 99,     // committed compression ledger
+  kConservation = 100,  // V_now - V0 - sum of ledgers at the last acceptance
+  kQuota = 101,         // request quota (>= 0 steps, < 0 minus a deadline)
+  kWarmUsed = 102,      // trials started from the learned warm start
+};
+
+struct MGLevelDev {
+  int nx, ny, nz, count;
+  int fx, fy, fz, aggregate;
+  int stencil;       // number of stencil offsets
+  int twidth;        // transfer-cache width
+  int off;           // offset of this level inside the per-field MG vectors
+  long long moff;    // offset of this level's canonical 125-slot matrix rows
+  long long eoff;    // offset of this level's ELL values
+  long long toff;    // offset of this level's transfer cache
+  int soff;          // offset of this level's stencil in the stencil table
+};
+
+struct Dev {
+  // grid
+  int nx, ny, nz;
+  long long N, NU, NV, NW, S, NF;
+  float hx, hy, hz;
+  float dtcfg;
+  float ox, oy, oz;
+  float eta0;
+  int px;
+  float slope, corr, corr_phase;
+  int shape;
+  float grav;
+  int max_face_cfl;
+  int hist_cap;
+  float wave[4];
+  float tol;
+  int linear_air, stokes2, flags;
+  int coastal;
+  float forcing[4];
+  float right_abs;
+  float cfl;
+  double cell_d;  // hx*hy*hz in double
+  // coastal zone: x columns [0, zone_x_end) hold every cell/face with a nonzero relaxation rate
+  int zone_x_end;
+
+  // physical banks [F | u | v | w | p]
+  float* bank0;
+  float* bank1;
+  // fine-grid work
+  float* r;      // residual
+  float* z;      // preconditioned residual
+  float* d;      // search direction
+  float* q;      // A d
+  float* diag;   // operator diagonal (work[12N] of the reference)
+  float* b;      // right-hand side
+  float* coef;   // 6 N face coefficients (face order -x,+x,-y,+y,-z,+z)
+  float* pbase;  // defect-correction base pressure (work[13N])
+  float* phi;    // signed distance
+  signed char* kind;  // -1 solid, 0 air, 1 wet
+  float4* plane;      // PLIC plane per cell
+  // motion work
+  float* mF;     // scratch F of sweep 1
+  float* mci;    // frozen compression indicator c_i
+  float* fwd;    // MacCormack forward value per face (also op 82 scratch)
+  float* tcache; // 6 faces: lo, hi, valid, start velocity xyz
+  int* src0;     // nearest-source banks
+  int* src1;
+  float* vband0; // valid band per bank
+  float* vband1;
+  float* pmask0; // pressure mask per bank
+  float* pmask1;
+  float4* history;   // 4 rows per trial
+  float4* chistory;  // 5 rows per step
+  // control and reductions
+  double* c;            // control block
+  double* part;         // per-block partials
+  unsigned int* count;  // last-block counters, one per reduction site
+  // solid table
+  const signed char* solid_tab;
+  int tab_w, tab_h;
+
+  // multigrid
+  int L;
+  MGLevelDev lv[kMaxLevels];
+  int mg_smoother, mg_smoothing, mg_mode, mg_lag, mg_aggr;
+  int bf16;                  // storage precision of the MG vectors/operators
+  void* mgv;                 // 8 fields x total_nodes (float or bf16): 0 rhs,1/2 x,3 active,4 scale,6 res,7 cheb d
+  long long mg_nodes;        // total nodes over all levels
+  float* mgmat;              // canonical 125-slot rows of levels >= 1 (FP32, build only)
+  void* mgell;               // ELL values [k][i] of levels >= 1 (float or bf16)
+  int* mgtid;                // transfer cache ids
+  float* mgtw;               // transfer cache weights
+  float* mglinv;             // dense L^-1 of the last level
+  float* snapshot;           // 9 N hierarchy snapshot
+  float* previous;           // 9 N previous-trial audit copy
+  void* c0;                  // 6 N level-0 face coefficients for the V-cycle (float or bf16)
+  unsigned int* hstate;      // hierarchy audit state
+  const int* stencil_tab;    // 3 ints per offset, all levels
+};
+
+// Reduction sites (one last-block counter each).
+enum Site {
+  kSiteCFL = 0,
+  kSiteCompress,
+  kSiteSweep,
+  kSiteCoastF,
+  kSiteCoastM,
+  kSiteBounds,
+  kSiteCGInit,
+  kSiteDot,
+  kSiteRZ,
+  kSiteAccept,
+  kSiteHS,
+  kSiteCount
+};
+
+}  // namespace wg

@@ -1,0 +1,728 @@
+// Multigrid preconditioner: hierarchy audit, Galerkin build and V-cycle
+// (neuron-forest/waves water/shaders/compute/pressure_multigrid.glslinc, pressure_mg_coarse.glslinc,
+// pressure_hierarchy_state.glsl; command order water/pressure_multigrid.gd:121-176).
+//
+// Storage type T is float (FP32 multigrid) or __nv_bfloat16 (BF16 storage and smoothing); every
+// arithmetic operation is FP32.  The Galerkin product is a deterministic gather: for coarse row I,
+// each thread of a group (the children of I in one (y, z) fine row) accumulates
+// (a_ij * w_iI) * w_jJ into its own shared-memory row of 125 slots, and the row is the sum of the
+// group partials in group order.  No float atomics touch any result.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wg {
+
+namespace {
+constexpr int NT = 256;
+constexpr int GT = 128;  // Galerkin block size
+
+DI bool build_on(const Dev& D) { return !(D.c[7] > .5) && !(D.c[5] < .5); }
+DI bool phase_on(const Dev& D, int phase) {
+  const double* c = D.c;
+  if (c[7] > .5) return false;
+  if (phase == 0) return (c[5] > .5 || c[57] == 2) && c[6] < .5;
+  return c[4] > .5 && c[6] < .5;
+}
+
+DI int pmod(int x, int m) { return x >= 0 ? x % m : (m - 1) - ((-1 - x) % m); }
+
+struct MG {
+  const Dev& D;
+  DI explicit MG(const Dev& d) : D(d) {}
+  DI const MGLevelDev& L(int l) const { return D.lv[l]; }
+  DI int wrap(int l, I3 q) const {
+    const MGLevelDev& v = D.lv[l];
+    q.z = pmod(q.z, v.nz);
+    if (D.px) q.x = pmod(q.x, v.nx);
+    if (q.x < 0 || q.x >= v.nx || q.y < 0 || q.y >= v.ny) return -1;
+    return q.x + v.nx * (q.y + v.ny * q.z);
+  }
+  DI I3 coord(int l, int i) const {
+    const MGLevelDev& v = D.lv[l];
+    return mk(i % v.nx, (i / v.nx) % v.ny, i / (v.nx * v.ny));
+  }
+  DI I3 delta(int l, int i, int j) const {
+    const MGLevelDev& v = D.lv[l];
+    I3 d = subI(coord(l, j), coord(l, i));
+    if (D.px) d.x = pmod(d.x + v.nx / 2, v.nx) - v.nx / 2;
+    d.z = pmod(d.z + v.nz / 2, v.nz) - v.nz / 2;
+    return d;
+  }
+  DI static int slot(I3 d) { return d.x + 2 + 5 * (d.y + 2 + 5 * (d.z + 2)); }
+  DI I3 offset(int l, int k) const {
+    const int* s = D.stencil_tab + 3 * (D.lv[l].soff + k);
+    return mk(__ldg(s), __ldg(s + 1), __ldg(s + 2));
+  }
+  template <class T> DI T* field(int f, int l) const { return (T*)D.mgv + (long long)f * D.mg_nodes + D.lv[l].off; }
+  template <class T> DI bool active(int l, int i) const { return i >= 0 && ld_val(field<T>(3, l)[i]) > .5f; }
+  DI float fine_coef(int f, int i) const { return D.snapshot[(long long)(f - 6) * D.N + i]; }
+  // coefficient (pressure_multigrid.glslinc:74-88), build-time values from the FP32 rows
+  template <class T> DI float coefficient(int l, int i, int j) const {
+    if (j < 0) return 0.f;
+    if (!active<T>(l, i) || !active<T>(l, j)) return i == j ? 1.f : 0.f;
+    if (l == 0) {
+      if (i == j) return fine_coef(12, i);
+      I3 q = coord(0, i);
+      float value = 0.f;
+      for (int axis = 0; axis < 3; axis++)
+        for (int side = 0; side < 2; side++)
+          if (wrap(0, ax(q, axis, 2 * side - 1)) == j) value -= fine_coef(6 + 2 * axis + side, i);
+      return value;
+    }
+    int a = min(i, j), b = max(i, j);
+    I3 d = delta(l, a, b);
+    if (abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2) return 0.f;
+    return D.mgmat[D.lv[l].moff + (long long)a * 125 + slot(d)];
+  }
+  DI bool unique_neighbor(int l, int i, I3 off, int j) const { return j >= 0 && eqI(delta(l, i, j), off); }
+  // compute_transfers (pressure_multigrid.glslinc:108-120)
+  template <class T> DI int compute_transfers(int l, int i, int* ids, float* ws) const {
+    const MGLevelDev& lv = D.lv[l];
+    const MGLevelDev& cv = D.lv[l + 1];
+    I3 q = coord(l, i);
+    int f[3] = {lv.fx, lv.fy, lv.fz};
+    if (lv.aggregate) {
+      int j = q.x / f[0] + cv.nx * (q.y / f[1] + cv.ny * (q.z / f[2]));
+      if (!active<T>(l + 1, j)) return 0;
+      ids[0] = j;
+      ws[0] = 1.f;
+      return 1;
+    }
+    float t[3];
+    int base[3];
+    for (int a = 0; a < 3; a++) {
+      float pos = ((float)q[a] + .5f) / (float)f[a] - .5f;
+      base[a] = (int)floorf(pos);
+      t[a] = fract_(pos);
+    }
+    int size = 0;
+    for (int z = 0; z < f[2]; z++)
+      for (int y = 0; y < f[1]; y++)
+        for (int x = 0; x < f[0]; x++) {
+          int bit[3] = {x, y, z};
+          I3 nb = mk(base[0] + x, base[1] + y, base[2] + z);
+          float w = 1.f;
+          for (int a = 0; a < 3; a++)
+            if (f[a] > 1) w *= bit[a] == 1 ? t[a] : 1.f - t[a];
+          if (nb.y >= cv.ny) continue;
+          nb.y = max(nb.y, 0);
+          nb.x = D.px ? pmod(nb.x, cv.nx) : min(max(nb.x, 0), cv.nx - 1);
+          nb.z = pmod(nb.z, cv.nz);
+          int j = nb.x + cv.nx * (nb.y + cv.ny * nb.z);
+          if (!active<T>(l + 1, j) || w == 0.f) continue;
+          ids[size] = j;
+          ws[size] = w;
+          size++;
+        }
+    return size;
+  }
+  DI int transfers(int l, int i, int* ids, float* ws) const {
+    const MGLevelDev& lv = D.lv[l];
+    int size = 0;
+    for (int k = 0; k < lv.twidth; k++) {
+      float w = D.mgtw[lv.toff + (long long)k * lv.count + i];
+      if (w > 0.f) {
+        ids[size] = D.mgtid[lv.toff + (long long)k * lv.count + i];
+        ws[size] = w;
+        size++;
+      }
+    }
+    return size;
+  }
+  // apply (pressure_multigrid.glslinc:90-105) with the V-cycle operators
+  template <class T> DI float apply(int l, int f, int i) const {
+    const T* x = field<T>(f, l);
+    if (!active<T>(l, i)) return ld_val(x[i]);
+    float sum = 0.f;
+    I3 q = coord(l, i);
+    if (l == 0) {
+      float here = ld_val(x[i]);
+      const T* c0 = (const T*)D.c0;
+      for (int axis = 0; axis < 3; axis++)
+        for (int side = 0; side < 2; side++) {
+          int j = wrap(0, ax(q, axis, 2 * side - 1));
+          float other = active<T>(0, j) ? ld_val(x[j]) : 0.f;
+          float k = ld_val(c0[(long long)(2 * axis + side) * D.N + i]);
+          sum += k * (here - other);
+        }
+      return sum;
+    }
+    const MGLevelDev& lv = D.lv[l];
+    const T* ell = (const T*)D.mgell + lv.eoff;
+    for (int k = 0; k < lv.stencil; k++) {
+      int j = wrap(l, addI(q, offset(l, k)));
+      sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[j > 0 ? j : 0]);
+    }
+    return sum;
+  }
+};
+
+// ---------------------------------------------------------------- hierarchy audit
+DI unsigned signature(const Dev& D, const Grid& g, long long i) {
+  if (D.kind[i] < 1) return 0;
+  I3 q = g.coord(i);
+  unsigned result = 0;
+  for (int axis = 0; axis < 3; axis++)
+    for (int side = 0; side < 2; side++) {
+      I3 nb = ax(q, axis, 2 * side - 1);
+      nb.z = pmod(nb.z, D.nz);
+      if (D.px) nb.x = pmod(nb.x, D.nx);
+      bool inside = nb.x >= 0 && nb.x < D.nx && nb.y >= 0 && nb.y < D.ny;
+      bool w = inside && D.kind[g.index3(nb)] > 0;
+      unsigned kind = D.coef[(long long)(2 * axis + side) * D.N + i] > 0.f ? (w ? 1u : 2u) : 0u;
+      result |= kind << (2 * (2 * axis + side));
+    }
+  return result;
+}
+__global__ void k_hs_reset(Dev D) {
+  if (!build_on(D)) return;
+  unsigned* s = D.hstate;
+  for (int k = 1; k <= 7; k++) s[k] = 0;
+  s[14] = s[0];
+  s[15] = 0;
+  s[16] = 0;
+  for (int k = 20; k < 32; k++) s[k] = 0;
+}
+struct AddU { DI unsigned operator()(unsigned a, unsigned b) const { return a + b; } };
+struct MaxU { DI unsigned operator()(unsigned a, unsigned b) const { return a < b ? b : a; } };
+__global__ void __launch_bounds__(NT) k_hs_count(Dev D) {
+  if (!build_on(D)) return;
+  __shared__ unsigned sh[32];
+  Grid g(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  // 1 kind!=snapshot, 2 signature diffs, 3 coefficient bit diffs, 4 kind!=previous,
+  // 5 signature diffs vs previous, 6 coefficient diffs vs previous, 7 max ratio bits, 15 invalid, 16 wet
+  unsigned a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < D.N) {
+    const float* cached = D.snapshot;
+    const float* prev = D.previous;
+    float kind = (float)D.kind[i];
+    a[0] = kind != cached[7 * D.N + i];
+    a[3] = kind != prev[7 * D.N + i];
+    a[8] = kind > .5f;
+    unsigned sig = signature(D, g, i), old = (unsigned)cached[8 * D.N + i], pv = (unsigned)prev[8 * D.N + i];
+    for (int face = 0; face < 6; face++) {
+      a[1] += ((sig >> (2 * face)) & 3u) != ((old >> (2 * face)) & 3u);
+      a[4] += ((sig >> (2 * face)) & 3u) != ((pv >> (2 * face)) & 3u);
+    }
+    float ratio = 0.f;
+    bool bad = false;
+    for (int k = 0; k < 7; k++) {
+      float value = k < 6 ? D.coef[(long long)k * D.N + i] : D.diag[i];
+      float was = cached[(long long)k * D.N + i];
+      a[2] += __float_as_uint(value) != __float_as_uint(was);
+      a[5] += __float_as_uint(value) != __float_as_uint(prev[(long long)k * D.N + i]);
+      if (was > 0.f) ratio = mxf(ratio, fabsf(value - was) / was);
+      if (isnan(value) || isinf(value) || value < 0.f) bad = true;
+    }
+    a[6] = __float_as_uint(ratio);
+    a[7] = bad ? 1u : 0u;
+  }
+  unsigned r[9];
+  for (int k = 0; k < 9; k++) r[k] = k == 6 ? block_reduce<NT>(a[k], MaxU(), sh) : block_reduce<NT>(a[k], AddU(), sh);
+  if (threadIdx.x == 0) {
+    unsigned* s = D.hstate;
+    const int dst[9] = {1, 2, 3, 4, 5, 6, 7, 15, 16};
+    for (int k = 0; k < 9; k++) {
+      if (k == 6) atomicMax(&s[7], r[k]);
+      else if (r[k]) atomicAdd(&s[dst[k]], r[k]);
+    }
+  }
+}
+__global__ void k_hs_decide(Dev D) {
+  if (!build_on(D)) return;
+  unsigned* s = D.hstate;
+  double* c = D.c;
+  if (s[15] > 0) { c[7] = 34; return; }
+  bool incompatible = s[0] == 0 || s[1] > 0 || s[2] > 0;
+  bool structural = D.mg_mode == 0 || incompatible;
+  bool numerical = D.mg_mode == 0 || incompatible || (s[3] > 0 && (D.mg_mode == 1 || s[10] + 1 >= (unsigned)D.mg_lag));
+  s[8] = numerical ? 1 : 0;
+  s[9] = structural ? 1 : 0;
+  s[10] = (numerical || s[3] == 0) ? 0 : s[10] + 1;
+  s[11] += s[8];
+  s[12] += s[9];
+  s[13] += 1;
+  s[0] = 1;
+  if (s[13] <= (unsigned)D.hist_cap) {
+    long long row = 64 + 32 * (long long)(s[13] - 1);
+    s[row] = s[13];
+    s[row + 1] = __float_as_uint((float)c[1]);
+    for (int k = 1; k <= 7; k++) s[row + 1 + k] = s[k];
+    s[row + 9] = s[8]; s[row + 10] = s[9]; s[row + 11] = s[10]; s[row + 12] = s[16]; s[row + 13] = s[11];
+  }
+}
+template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(Dev D) {
+  if (!build_on(D)) return;
+  Grid g(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  bool num = D.hstate[8] != 0;
+  for (int k = 0; k < 7; k++) {
+    float value = k < 6 ? D.coef[(long long)k * D.N + i] : D.diag[i];
+    D.previous[(long long)k * D.N + i] = value;
+    if (num) D.snapshot[(long long)k * D.N + i] = value;
+  }
+  float kind = (float)D.kind[i], sig = (float)signature(D, g, i);
+  D.previous[7 * D.N + i] = kind;
+  D.previous[8 * D.N + i] = sig;
+  if (num) {
+    D.snapshot[7 * D.N + i] = kind;
+    D.snapshot[8 * D.N + i] = sig;
+    if (D.bf16) {
+      T* c0 = (T*)D.c0;
+      for (int k = 0; k < 6; k++) c0[(long long)k * D.N + i] = st_val<T>(D.coef[(long long)k * D.N + i]);
+    }
+  }
+}
+__global__ void k_hs_record(Dev D) {
+  if (!build_on(D)) return;
+  unsigned* s = D.hstate;
+  if (s[13] <= (unsigned)D.hist_cap) {
+    long long row = 64 + 32 * (long long)(s[13] - 1);
+    for (int l = 0; l < 12; l++) s[row + 16 + l] = s[20 + l];
+  }
+}
+
+// ---------------------------------------------------------------- build ops
+template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(Dev D, int l) {
+  if (!build_on(D) || D.hstate[9] == 0) return;
+  __shared__ unsigned sh[32];
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  const MGLevelDev& lv = D.lv[l];
+  unsigned changed = 0;
+  if (i < lv.count) {
+    float value = 0.f;
+    if (l == 0) value = D.kind[i] > 0 ? 1.f : 0.f;
+    else {
+      const MGLevelDev& pv = D.lv[l - 1];
+      I3 base = m.coord(l, i);
+      base = mk(base.x * pv.fx, base.y * pv.fy, base.z * pv.fz);
+      for (int z = 0; z < pv.fz; z++)
+        for (int y = 0; y < pv.fy; y++)
+          for (int x = 0; x < pv.fx; x++)
+            if (m.active<T>(l - 1, m.wrap(l - 1, addI(base, mk(x, y, z))))) value = 1.f;
+    }
+    T* f3 = m.field<T>(3, l);
+    if (ld_val(f3[i]) != value) changed = 1;
+    f3[i] = st_val<T>(value);
+  }
+  unsigned r = block_reduce<NT>(changed, AddU(), sh);
+  if (threadIdx.x == 0 && r) atomicAdd(&D.hstate[20 + l], r);
+}
+template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(Dev D, int l) {
+  if (!build_on(D) || !(D.hstate[14] == 0 || D.hstate[20 + l + 1] != 0)) return;
+  MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= lv.count) return;
+  int ids[8];
+  float ws[8];
+  int size = m.compute_transfers<T>(l, i, ids, ws);
+  for (int k = 0; k < lv.twidth; k++) {
+    D.mgtid[lv.toff + (long long)k * lv.count + i] = k < size ? ids[k] : 0;
+    D.mgtw[lv.toff + (long long)k * lv.count + i] = k < size ? ws[k] : 0.f;
+  }
+}
+// l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
+template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(Dev D, int l) {
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= lv.count) return;
+  float sum = 0.f;
+  I3 q = m.coord(l, i);
+  if (l == 0) {
+    sum = m.fine_coef(12, i);
+    for (int axis = 0; axis < 3; axis++)
+      for (int side = 0; side < 2; side++)
+        if (m.active<T>(0, m.wrap(0, ax(q, axis, 2 * side - 1)))) sum += m.fine_coef(6 + 2 * axis + side, i);
+  } else {
+    for (int k = 0; k < lv.stencil; k++) {
+      I3 off = m.offset(l, k);
+      int j = m.wrap(l, addI(q, off));
+      if (m.unique_neighbor(l, i, off, j)) sum += fabsf(m.coefficient<T>(l, i, j));
+    }
+  }
+  if (!(sum > 0.f) || isnan(sum) || isinf(sum)) {
+    D.c[7] = 32;
+    return;
+  }
+  m.field<T>(4, l)[i] = st_val<T>(1.f / sum);
+}
+// Children box of coarse coordinate qc along one axis of fine level l.
+DI void child_range(const Dev& D, int l, int axis, int qc, int& lo, int& ext) {
+  const MGLevelDev& lv = D.lv[l];
+  int f = axis == 0 ? lv.fx : (axis == 1 ? lv.fy : lv.fz);
+  int nf = axis == 0 ? lv.nx : (axis == 1 ? lv.ny : lv.nz);
+  if (lv.aggregate || f == 1) { lo = qc * f; ext = f; return; }
+  lo = qc * f - 1;
+  ext = 4;
+  bool periodic = axis == 2 || (axis == 0 && D.px);
+  if (periodic && nf <= 4) { lo = 0; ext = nf; }
+}
+// Deterministic Galerkin product of level l into level l+1 (replaces ops 2 + 3).
+template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(Dev D, int l, int ex, int ey, int ez) {
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  extern __shared__ float part[];  // [125][GT]
+  MG m(D);
+  const int G = ey * ez, rpb = GT / G;
+  const MGLevelDev& fl = D.lv[l];
+  const MGLevelDev& cl = D.lv[l + 1];
+  const int t = threadIdx.x;
+  for (int s = 0; s < 125; s++) part[s * GT + t] = 0.f;
+  int row_local = t / G, g = t % G;
+  int I = blockIdx.x * rpb + row_local;
+  if (row_local < rpb && I < cl.count && m.active<T>(l + 1, I)) {
+    I3 qc = m.coord(l + 1, I);
+    int lo[3], ext[3];
+    for (int a = 0; a < 3; a++) child_range(D, l, a, qc[a], lo[a], ext[a]);
+    int gz = g / ey, gy = g % ey;
+    for (int gx = 0; gx < ext[0]; gx++) {
+      int i = m.wrap(l, mk(lo[0] + gx, lo[1] + gy, lo[2] + gz));
+      if (i < 0 || !m.active<T>(l, i)) continue;
+      int li[8], ri[8];
+      float lw[8], rw[8];
+      int nl = m.transfers(l, i, li, lw);
+      I3 qi = m.coord(l, i);
+      for (int a = 0; a < nl; a++) {
+        if (li[a] != I) continue;
+        for (int k = 0; k < fl.stencil; k++) {
+          I3 off = m.offset(l, k);
+          int j = m.wrap(l, addI(qi, off));
+          if (j < 0 || !m.active<T>(l, j)) continue;
+          if (l > 0 && !m.unique_neighbor(l, i, off, j)) continue;
+          float aij = l == 0 ? (k == 0 ? m.fine_coef(12, i) : -m.fine_coef(5 + k, i)) : m.coefficient<T>(l, i, j);
+          if (aij == 0.f) continue;
+          int nr = m.transfers(l, j, ri, rw);
+          float al = aij * lw[a];
+          for (int b = 0; b < nr; b++) {
+            I3 d = m.delta(l + 1, I, ri[b]);
+            if (abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2) {
+              D.c[7] = 31;
+              continue;
+            }
+            part[MG::slot(d) * GT + t] += al * rw[b];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int u = t; u < rpb * 125; u += GT) {
+    int rl = u / 125, s = u % 125;
+    int row = blockIdx.x * rpb + rl;
+    if (row >= cl.count) continue;
+    float total = 0.f;
+    for (int gg = 0; gg < G; gg++) total += part[s * GT + rl * G + gg];
+    I3 d = mk(s % 5 - 2, (s / 5) % 5 - 2, s / 25 - 2);
+    int J = m.wrap(l + 1, addI(m.coord(l + 1, row), d));
+    bool canonical = J >= row && eqI(m.delta(l + 1, row, J), d) && m.active<T>(l + 1, row);
+    D.mgmat[cl.moff + (long long)row * 125 + s] = canonical ? total : 0.f;
+  }
+}
+// ELL rows (pressure_multigrid.glslinc:176-182)
+template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(Dev D, int l) {
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= lv.count) return;
+  I3 q = m.coord(l, i);
+  T* ell = (T*)D.mgell + lv.eoff;
+  for (int k = 0; k < lv.stencil; k++) {
+    I3 off = m.offset(l, k);
+    int j = m.wrap(l, addI(q, off));
+    float a = m.unique_neighbor(l, i, off, j) ? m.coefficient<T>(l, i, j) : 0.f;
+    ell[(long long)k * lv.count + i] = st_val<T>(a);
+  }
+}
+// Dense Cholesky and L^-1 of the last level (pressure_mg_coarse.glslinc:34-48), one block.
+template <class T> __global__ void k_mg_chol(Dev D, int l) {
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  __shared__ float dense[64 * 64];
+  __shared__ float inv[64 * 64];
+  MG m(D);
+  const int n = D.lv[l].count;
+  const int t = threadIdx.x;
+  for (int k = t; k < n * n; k += blockDim.x) dense[k] = m.coefficient<T>(l, k / n, k % n);
+  __syncthreads();
+  for (int k = 0; k < n; k++) {
+    if (t == 0) {
+      float d = dense[k * n + k];
+      for (int j = 0; j < k; j++) d -= dense[k * n + j] * dense[k * n + j];
+      if (!(d > 0.f) || isnan(d) || isinf(d)) {
+        D.c[7] = 33;
+        d = 1.f;
+      }
+      dense[k * n + k] = sqrtf(d);
+    }
+    __syncthreads();
+    if (t > k && t < n) {
+      float e = dense[t * n + k];
+      for (int j = 0; j < k; j++) e -= dense[t * n + j] * dense[k * n + j];
+      dense[t * n + k] = e / dense[k * n + k];
+    }
+    __syncthreads();
+  }
+  for (int row = 0; row < n; row++) {
+    if (t < n) {
+      float d = t == row ? 1.f : 0.f;
+      for (int j = 0; j < row; j++) d -= dense[row * n + j] * inv[j * n + t];
+      inv[row * n + t] = d / dense[row * n + row];
+    }
+    __syncthreads();
+  }
+  for (int k = t; k < n * n; k += blockDim.x) D.mglinv[k] = inv[k];
+}
+
+// ---------------------------------------------------------------- V-cycle
+template <class T> __global__ void __launch_bounds__(NT) k_mg_load(Dev D, int phase) {
+  if (!phase_on(D, phase)) return;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  T* v = (T*)D.mgv;
+  long long M = D.mg_nodes;
+  v[i] = st_val<T>(D.r[i]);
+  v[M + i] = st_val<T>(0.f);
+  v[2 * M + i] = st_val<T>(0.f);
+}
+// 4th-kind Chebyshev sweep k (pressure_multigrid.glslinc:192-196)
+template <class T> __global__ void __launch_bounds__(NT) k_mg_cheb(Dev D, int phase, int l, int source, int k) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  float c1 = (float)(2 * k - 3) / (float)(2 * k + 1), c2 = (float)(8 * k - 4) / (float)(2 * k + 1);
+  float r = ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, source, i);
+  T* v7 = m.field<T>(7, l);
+  float d = (k == 1 ? 0.f : c1 * ld_val(v7[i])) + c2 * ld_val(m.field<T>(4, l)[i]) * r;
+  float x = ld_val(m.field<T>(source, l)[i]) + d;
+  v7[i] = st_val<T>(d);
+  m.field<T>(3 - source, l)[i] = st_val<T>(x);
+}
+// Jacobi sweeps: op 14 (first, from zero) and op 6
+template <class T> __global__ void __launch_bounds__(NT) k_mg_jacobi(Dev D, int phase, int l, int source, int first) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  float s = ld_val(m.field<T>(4, l)[i]), b = ld_val(m.field<T>(0, l)[i]);
+  if (first) m.field<T>(2, l)[i] = st_val<T>(s * b);
+  else m.field<T>(3 - source, l)[i] = st_val<T>(ld_val(m.field<T>(source, l)[i]) + s * (b - m.apply<T>(l, source, i)));
+}
+// op 7: residual
+template <class T> __global__ void __launch_bounds__(NT) k_mg_residual(Dev D, int phase, int l, int f) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  m.field<T>(6, l)[i] = st_val<T>(ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, f, i));
+}
+// op 8: exact P^T restriction into level l (pressure_multigrid.glslinc:200-224)
+template <class T> __global__ void __launch_bounds__(NT) k_mg_restrict(Dev D, int phase, int l) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  const MGLevelDev& cv = D.lv[l];
+  if (i >= cv.count) return;
+  const int parent = l - 1;
+  const MGLevelDev& pv = D.lv[parent];
+  int f[3] = {pv.fx, pv.fy, pv.fz}, nf[3] = {pv.nx, pv.ny, pv.nz}, nc[3] = {cv.nx, cv.ny, cv.nz};
+  const T* r6 = m.field<T>(6, parent);
+  float sum = 0.f;
+  I3 qc = m.coord(l, i);
+  if (m.active<T>(l, i)) {
+    if (pv.aggregate) {
+      for (int z = 0; z < f[2]; z++)
+        for (int y = 0; y < f[1]; y++)
+          for (int x = 0; x < f[0]; x++) {
+            int j = m.wrap(parent, mk(qc.x * f[0] + x, qc.y * f[1] + y, qc.z * f[2] + z));
+            if (m.active<T>(parent, j)) sum += ld_val(r6[j]);
+          }
+    } else {
+      int lo[3] = {qc.x * f[0], qc.y * f[1], qc.z * f[2]}, ext[3] = {1, 1, 1};
+      for (int a = 0; a < 3; a++)
+        if (f[a] > 1) {
+          lo[a]--;
+          ext[a] = 4;
+          if ((a == 2 || (a == 0 && D.px)) && nf[a] <= 4) { lo[a] = 0; ext[a] = nf[a]; }
+        }
+      for (int z = 0; z < ext[2]; z++)
+        for (int y = 0; y < ext[1]; y++)
+          for (int x = 0; x < ext[0]; x++) {
+            int j = m.wrap(parent, mk(lo[0] + x, lo[1] + y, lo[2] + z));
+            if (!m.active<T>(parent, j)) continue;
+            I3 q = m.coord(parent, j);
+            float weight = 1.f;
+            for (int a = 0; a < 3; a++) {
+              float pos = ((float)q[a] + .5f) / (float)f[a] - .5f;
+              int base = (int)floorf(pos);
+              float t = fract_(pos);
+              float w = 0.f;
+              for (int bit = 0; bit < f[a]; bit++) {
+                int nb = base + bit;
+                if (a == 2 || (a == 0 && D.px)) nb = pmod(nb, nc[a]);
+                else if (a == 0) nb = min(max(nb, 0), nc[a] - 1);
+                else nb = max(nb, 0);
+                if (nb == qc[a]) w += f[a] == 1 ? 1.f : (bit == 1 ? t : 1.f - t);
+              }
+              weight *= w;
+            }
+            sum += weight * ld_val(r6[j]);
+          }
+    }
+  }
+  m.field<T>(0, l)[i] = st_val<T>(sum);
+  m.field<T>(1, l)[i] = st_val<T>(0.f);
+  m.field<T>(2, l)[i] = st_val<T>(0.f);
+}
+// op 9: prolongation-add
+template <class T> __global__ void __launch_bounds__(NT) k_mg_prolong(Dev D, int phase, int l, int ff, int cf) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  float add = 0.f;
+  if (m.active<T>(l, i)) {
+    int ids[8];
+    float ws[8];
+    int size = m.transfers(l, i, ids, ws);
+    const T* xc = m.field<T>(cf, l + 1);
+    for (int k = 0; k < size; k++) add += ws[k] * ld_val(xc[ids[k]]);
+  }
+  T* x = m.field<T>(ff, l);
+  x[i] = st_val<T>(ld_val(x[i]) + add);
+}
+// op 12: coarse solve x = L^-T (L^-1 b), one block
+template <class T> __global__ void k_mg_coarse(Dev D, int phase, int l) {
+  if (!phase_on(D, phase)) return;
+  __shared__ float small[64];
+  MG m(D);
+  const int n = D.lv[l].count, t = threadIdx.x;
+  const T* b = m.field<T>(0, l);
+  if (t < n) {
+    float d = 0.f;
+    for (int j = 0; j <= t; j++) d += D.mglinv[t * n + j] * ld_val(b[j]);
+    small[t] = d;
+  }
+  __syncthreads();
+  if (t < n) {
+    float d = 0.f;
+    for (int j = t; j < n; j++) d += D.mglinv[j * n + t] * small[j];
+    m.field<T>(1, l)[t] = st_val<T>(d);
+  }
+}
+// op 10 of the cycle + op 4 / op 9 finalisation
+template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(Dev D, int phase, int f) {
+  if (!phase_on(D, phase)) return;
+  MG m(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[4] = {0, 0, 0, 0};
+  if (i < D.N) {
+    float r = D.r[i], z = ld_val(m.field<T>(f, 0)[i]), b = D.b[i];
+    D.z[i] = z;
+    if (phase == 0) D.d[i] = z;
+    v[0] = (double)r * (double)z;
+    v[1] = (double)r * (double)r;
+    v[2] = (double)b * (double)b;
+    v[3] = (double)fabsf(r);
+  }
+  const int ops[4] = {0, 0, 0, 1};
+  double out[4];
+  if (last_block_reduce<NT, 4>(D, kSiteRZ, v, ops, out) && threadIdx.x == 0) {
+    if (phase == 0) finalize_op4(D, out);
+    else finalize_op9(D, out);
+  }
+}
+
+unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
+
+template <class T> struct Cycle {
+  const Dev& D;
+  cudaStream_t s;
+  int phase;
+  int smooth(int l, int field, bool zero) {
+    unsigned gr = grid_for(D.lv[l].count);
+    for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
+      if (D.mg_smoother == 1) k_mg_cheb<T><<<gr, NT, 0, s>>>(D, phase, l, field, sweep + 1);
+      else k_mg_jacobi<T><<<gr, NT, 0, s>>>(D, phase, l, field, zero && sweep == 0 ? 1 : 0);
+      field = 3 - field;
+    }
+    return field;
+  }
+  int level(int l) {
+    unsigned gr = grid_for(D.lv[l].count);
+    if (l == D.L - 1) {
+      if (D.lv[l].count <= 64) {
+        k_mg_coarse<T><<<1, 64, 0, s>>>(D, phase, l);
+        return 1;
+      }
+      int tf = 1;
+      for (int sweep = 0; sweep < 32; sweep++) {
+        k_mg_jacobi<T><<<gr, NT, 0, s>>>(D, phase, l, tf, sweep == 0 ? 1 : 0);
+        tf = 3 - tf;
+      }
+      return tf;
+    }
+    int field = smooth(l, 1, true);
+    k_mg_residual<T><<<gr, NT, 0, s>>>(D, phase, l, field);
+    k_mg_restrict<T><<<grid_for(D.lv[l + 1].count), NT, 0, s>>>(D, phase, l + 1);
+    int cf = level(l + 1);
+    k_mg_prolong<T><<<gr, NT, 0, s>>>(D, phase, l, field, cf);
+    return smooth(l, field, false);
+  }
+  void run() {
+    if (phase == 0) k_mg_load<T><<<grid_for(D.N), NT, 0, s>>>(D, phase);
+    int f = level(0);
+    k_mg_finish<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, f);
+  }
+};
+
+template <class T> void build(const Dev& D, cudaStream_t s) {
+  k_hs_reset<<<1, 1, 0, s>>>(D);
+  k_hs_count<<<grid_for(D.N), NT, 0, s>>>(D);
+  k_hs_decide<<<1, 1, 0, s>>>(D);
+  k_hs_snapshot<T><<<grid_for(D.N), NT, 0, s>>>(D);
+  for (int l = 0; l < D.L; l++) k_mg_mask<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  for (int l = 0; l + 1 < D.L; l++) k_mg_transfer<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  k_mg_scale<T><<<grid_for(D.lv[0].count), NT, 0, s>>>(D, 0);
+  for (int l = 1; l < D.L; l++) {
+    int lo, ext[3];
+    // the children box extents of fine level l-1 are the same for every coarse row
+    for (int a = 0; a < 3; a++) {
+      const MGLevelDev& lv = D.lv[l - 1];
+      int f = a == 0 ? lv.fx : (a == 1 ? lv.fy : lv.fz);
+      int nf = a == 0 ? lv.nx : (a == 1 ? lv.ny : lv.nz);
+      bool periodic = a == 2 || (a == 0 && D.px);
+      ext[a] = (lv.aggregate || f == 1) ? f : ((periodic && nf <= 4) ? nf : 4);
+    }
+    (void)lo;
+    int G = ext[1] * ext[2], rpb = GT / G;
+    unsigned gr = (unsigned)((D.lv[l].count + rpb - 1) / rpb);
+    k_mg_galerkin<T><<<gr, GT, 125 * GT * sizeof(float), s>>>(D, l - 1, ext[0], ext[1], ext[2]);
+    k_mg_scale<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  }
+  for (int l = 1; l < D.L; l++) k_mg_ell<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  if (D.lv[D.L - 1].count <= 64) k_mg_chol<T><<<1, 64, 0, s>>>(D, D.L - 1);
+  k_hs_record<<<1, 1, 0, s>>>(D);
+}
+
+}  // namespace
+
+void mg_kernel_attributes() {
+  cudaFuncSetAttribute(k_mg_galerkin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
+  cudaFuncSetAttribute(k_mg_galerkin<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
+}
+void launch_mg_build(const Dev& D, cudaStream_t s) {
+  if (D.bf16) build<__nv_bfloat16>(D, s);
+  else build<float>(D, s);
+}
+void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase) {
+  if (D.bf16) Cycle<__nv_bfloat16>{D, s, phase}.run();
+  else Cycle<float>{D, s, phase}.run();
+}
+
+}  // namespace wg

@@ -1,0 +1,561 @@
+// Motion phase of the solver step: CFL time step, compression pre-check, the three directional
+// PLIC/Weymouth-Yue VOF sweeps and limited MacCormack advection
+// (neuron-forest/waves water/shaders/compute/coupled_motion.glslinc ops 20-28, 45/46, 55/56).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wg {
+
+namespace {
+constexpr int NT = 256;
+
+struct Motion {
+  const Dev& D;
+  Grid g;
+  Coast cs;
+  int acc, cand;
+  const float* A;  // accepted bank
+  float* Cb;       // candidate bank
+  float dt;
+  double c1;
+  DI explicit Motion(const Dev& d) : D(d), g(d), cs(d) {
+    acc = acc_bank(d);
+    cand = 1 - acc;
+    A = bank_ptr(d, acc);
+    Cb = bank_ptr(d, cand);
+    dt = (float)d.c[20];
+    c1 = d.c[1];
+  }
+  // old_face (coupled_motion.glslinc:28-35)
+  DI float old_face(I3 q, int axis) const {
+    q = g.wrap_face(q);
+    if (D.coastal && q.x < 0 && !g.wall_face(q, axis)) return cs.velocity_c(cs.face_position(g, q, axis), (float)c1, axis);
+    if (!g.face_in_bounds(q, axis) || g.wall_face(q, axis)) return 0.f;
+    return A[g.face_index(q, axis)];
+  }
+  DI float face_courant(I3 q, int axis) const { return old_face(q, axis) * dt / g.h(axis); }
+  // transport_f (coupled_motion.glslinc:36-44)
+  DI float transport_f(I3 q) const {
+    q = g.wrap_cell(q);
+    if (D.coastal && q.x < 0 && !g.solid(q)) return cs.fraction(g, q, (float)c1);
+    if (g.outside(q) || g.solid(q)) return 0.f;
+    long long i = g.index3(q);
+    int sweep = (int)D.c[21];
+    return sweep == 0 ? A[i] : (sweep == 1 ? Cb[i] : D.mF[i]);
+  }
+  // courant_at (coupled_motion.glslinc:189-202)
+  DI float courant_at(I3 q, const float* B, bool accelerate) const {
+    float s[3];
+    for (int axis = 0; axis < 3; axis++) {
+      I3 r = ax(q, axis, 1);
+      s[axis] = mxf(fabsf(B[g.face_index(q, axis)]), fabsf(B[g.face_index(r, axis)]));
+    }
+    if (D.coastal && accelerate) {
+      F3 cq = g.center(q);
+      float tt = (float)(c1 + (double)D.dtcfg);
+      if (cs.rate(cq.x) > 0.f) {
+        float s0, s1;
+        cs.surface(cq.x, tt, s0, s1);
+        if (cq.y < s0 + 3.f * D.hy) {
+          for (int axis = 0; axis < 3; axis++) {
+            I3 r = ax(q, axis, 1);
+            s[axis] = mxf(s[axis], mxf(fabsf(cs.velocity_c(cs.face_position(g, q, axis), tt, axis)),
+                                       fabsf(cs.velocity_c(cs.face_position(g, r, axis), tt, axis))));
+          }
+        }
+      }
+    }
+    if (accelerate) s[1] += 9.81f * D.dtcfg * D.grav;
+    s[0] = s[0] / D.hx;
+    s[1] = s[1] / D.hy;
+    s[2] = s[2] / D.hz;
+    return D.max_face_cfl ? mxf(s[0], mxf(s[1], s[2])) : s[0] * 1.f + s[1] * 1.f + s[2] * 1.f;
+  }
+};
+
+DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
+
+// ---------------------------------------------------------------- op 20/21
+__global__ void __launch_bounds__(NT) k_cfl(Dev D) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[1] = {0.0};
+  if (i < D.N) v[0] = (double)m.courant_at(m.g.coord(i), m.A, true);
+  const int ops[1] = {1};
+  double out[1];
+  if (last_block_reduce<NT, 1>(D, kSiteCFL, v, ops, out) && threadIdx.x == 0) {
+    double* c = D.c;
+    float rate = mxf(0.f, (float)out[0]);
+    float d = mnf(D.dtcfg, D.cfl / mxf(rate, 1e-20f));
+    if (c[29] > 0) d = mnf(d, (float)c[30]);
+    c[20] = (double)d;
+    c[21] = 0; c[22] = 0; c[23] = 0; c[39] = 0; c[kSweepRound] = 0; c[kSweepComp] = 0;
+    if (D.coastal)
+      for (int f = 64; f < 70; f++) c[f] = 0;
+  }
+}
+
+// ---------------------------------------------------------------- op 45/46 + c_i of op 22
+__global__ void __launch_bounds__(NT) k_compress(Dev D) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  const float* pmA = m.acc == 0 ? D.pmask0 : D.pmask1;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[4] = {0, 0, 0, 0};
+  if (i < D.N) {
+    I3 q = m.g.coord(i);
+    float f = m.A[i];
+    float dv = 0.f, raw = 0.f;
+    for (int axis = 0; axis < 3; axis++) {
+      I3 r = ax(q, axis, 1);
+      float h = m.g.h(axis);
+      dv += (m.old_face(r, axis) - m.old_face(q, axis)) / h;
+      raw += (m.A[m.g.face_index(r, axis)] - m.A[m.g.face_index(q, axis)]) / h;
+    }
+    if (f > .5f) v[0] = (double)(m.dt * dv) * D.cell_d;
+    if (f > .5f && pmA[i] < .5f) v[1] = 1.0;
+    v[2] = (double)f * D.cell_d;
+    if (f > .5f) v[3] = (double)(m.dt * raw) * D.cell_d;
+    D.mci[i] = f > .5f ? 1.f : 0.f;
+  }
+  const int ops[4] = {0, 0, 0, 0};
+  double out[4];
+  if (last_block_reduce<NT, 4>(D, kSiteCompress, v, ops, out) && threadIdx.x == 0) {
+    double* c = D.c;
+    c[35] = out[0]; c[36] = out[1]; c[37] = out[2]; c[38] = out[3];
+    if (out[1] > 0) { c[7] = 22; c[3] += 1; }
+  }
+}
+
+// ---------------------------------------------------------------- op 23
+__global__ void __launch_bounds__(NT) k_sweep_plane(Dev D) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  I3 q = m.g.coord(i);
+  float f = m.transport_f(q);
+  float4 out;
+  if (f <= 0.f || f >= 1.f) out = make_float4(0.f, 1.f, 0.f, f);
+  else {
+    auto fr = [&](I3 p) { return m.transport_f(p); };
+    F3 grad = interface_gradient(m.g, q, fr);
+    if (D.flags & 1) grad = height_normal(m.g, q, grad, fr);
+    out = plane_from_gradient(D, grad, f);
+  }
+  D.plane[i] = out;
+}
+
+// op 24 flux of one sweep-axis face (coupled_motion.glslinc:375-388)
+DI float sweep_flux(const Motion& m, I3 q, int axis) {
+  const Dev& D = m.D;
+  if (m.g.wall_face(q, axis)) return 0.f;
+  float velocity = m.old_face(q, axis), courant = m.face_courant(q, axis);
+  I3 donor = q;
+  if (velocity > 0.f) donor[axis]--;
+  donor = m.g.wrap_cell(donor);
+  float f = m.transport_f(donor), width = fabsf(courant);
+  float amount = f * width;
+  if (f > 0.f && f < 1.f && width > 0.f) {
+    float4 eq = (D.coastal && donor.x < 0) ? m.cs.plane(m.g, donor, (float)m.c1) : D.plane[m.g.index3(donor)];
+    F3 n = mf(eq.x, eq.y, eq.z);
+    F3 low = mf(0.f, 0.f, 0.f), extent = mf(1.f, 1.f, 1.f);
+    extent[axis] = width;
+    if (velocity > 0.f) low[axis] = 1.f - width;
+    amount = width * cube_volume(mul3(n, extent), eq.w - dot3(n, low));
+  }
+  return amount * sgnf(velocity);
+}
+
+// ---------------------------------------------------------------- op 24 + 55/56 + 25/26
+__global__ void __launch_bounds__(NT) k_sweep_update(Dev D) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  int sa = ((int)D.c[2] + (int)D.c[21]) % 3;
+  int sweep = (int)D.c[21];
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  // reductions: -min f, max f, sum change, sum |change|, rounding ledger, compression, top, in, out
+  double v[9] = {-1e20, -1e20, 0, 0, 0, 0, 0, 0, 0};
+  if (i < D.N) {
+    I3 q = m.g.coord(i), r = ax(q, sa, 1);
+    float fq = sweep_flux(m, q, sa), fr_ = sweep_flux(m, r, sa);
+    float net = fq - fr_;
+    float correction = D.mci[i] * (m.face_courant(r, sa) - m.face_courant(q, sa));
+    float increment = net + correction;
+    float fin = m.transport_f(q);
+    float f = fin + increment;
+    float change = 0.f;
+    if (f >= -1e-6f && f <= 1.f + 1e-6f) change = clampf_(f, 0.f, 1.f) - f;
+    float out = f + change;
+    if (sweep == 1) D.mF[i] = out;
+    else m.Cb[i] = out;
+    float a = f, b = f;
+    if (isnan(f) || isinf(f)) { a = -1e30f; b = 1e30f; }
+    v[0] = -(double)a;
+    v[1] = (double)b;
+    v[2] = (double)change;
+    v[3] = (double)fabsf(change);
+    v[4] = ((double)out - (double)fin - (double)net - (double)correction) * D.cell_d;
+    v[5] = (double)correction * D.cell_d;
+    if (sa == 1 && q.y == D.ny - 1) v[6] = (double)fr_ * D.cell_d;
+    if (D.coastal && sa == 0 && q.x == 0) {
+      double fl = (double)fq * D.cell_d;
+      v[7] = fl > 0 ? fl : 0.0;
+      v[8] = -fl > 0 ? -fl : 0.0;
+    }
+  }
+  const int ops[9] = {1, 1, 0, 0, 0, 0, 0, 0, 0};
+  double out[9];
+  if (last_block_reduce<NT, 9>(D, kSiteSweep, v, ops, out) && threadIdx.x == 0) {
+    double* c = D.c;
+    float vmin = (float)(-out[0]), vmax = (float)out[1];
+    long long step = (long long)c[32] - 1;
+    if (c[32] >= 1 && step < D.hist_cap) D.history[step * 4 + sweep] = make_float4(vmin, vmax, (float)out[2], (float)out[3]);
+    c[22] += out[2] * D.cell_d;
+    c[23] += out[3] * D.cell_d;
+    c[kSweepRound] += out[4];
+    c[kSweepComp] += out[5];
+    c[39] += out[6];
+    if (D.coastal) { c[65] += out[7]; c[66] += out[8]; }
+    if (vmin < -1e-6f || vmax > 1.f + 1e-6f) { c[7] = 10 + c[21]; c[3] += 1; }
+    c[21] += 1;
+  }
+}
+
+// ---------------------------------------------------------------- MacCormack
+struct Mac {
+  const Motion& m;
+  const float* vb;  // valid band of the accepted bank
+  DI explicit Mac(const Motion& mm) : m(mm) { vb = mm.acc == 0 ? mm.D.vband0 : mm.D.vband1; }
+  // reflect_voxel_donor (coupled_motion.glslinc:66-85)
+  __device__ __noinline__ bool reflect(I3& q, int component, float& parity) const {
+    const Grid& g = m.g;
+    float best = 1e20f;
+    I3 selected = q;
+    parity = 1.f;
+    for (int axis = 0; axis < 3; axis++)
+      for (int sign = -1; sign <= 1; sign += 2) {
+        for (int layer = 1; layer <= 3; layer++) {
+          I3 edge = g.wrap_face(ax(q, axis, sign * layer));
+          if (!g.face_in_bounds(edge, component)) break;
+          I3 left = ax(edge, component, -1);
+          bool sl = g.solid(left), sr = g.solid(edge);
+          bool boundary = axis == component ? (sl != sr) : (!sl && !sr);
+          if (!boundary) continue;
+          I3 mirror = g.wrap_face(ax(q, axis, sign * (2 * layer - (axis == component ? 0 : 1))));
+          float distance = ((float)layer - (axis == component ? 0.f : .5f)) * g.h(axis);
+          if (g.face_in_bounds(mirror, component) && !g.wall_face(mirror, component) && distance < best) {
+            selected = mirror;
+            best = distance;
+            parity = axis == component ? -1.f : 1.f;
+          }
+          break;
+        }
+      }
+    q = selected;
+    return best < 1e19f;
+  }
+  // velocity_donor (coupled_motion.glslinc:86-111)
+  __device__ __noinline__ float donor(I3 q, int axis, bool forward, bool& valid) const {
+    const Grid& g = m.g;
+    const Dev& D = m.D;
+    float parity = 1.f;
+    if (q.y < 0) {
+      q.y = -q.y - (axis == 1 ? 0 : 1);
+      if (axis == 1) parity = -parity;
+    }
+    if (!D.px) {
+      if (!D.coastal && q.x < 0) {
+        q.x = -q.x - (axis == 0 ? 0 : 1);
+        if (axis == 0) parity = -parity;
+      }
+      if (q.x >= D.nx + (axis == 0 ? 1 : 0)) {
+        q.x = 2 * D.nx - q.x - (axis == 0 ? 0 : 1);
+        if (axis == 0) parity = -parity;
+      }
+    }
+    q = g.wrap_face(q);
+    if (D.coastal && q.x < 0 && q.y >= 0 && q.y < D.ny && !g.wall_face(q, axis)) {
+      valid = true;
+      return parity * m.cs.velocity_c(m.cs.face_position(g, q, axis), (float)m.c1, axis);
+    }
+    if (!g.face_in_bounds(q, axis)) {
+      valid = false;
+      return 0.f;
+    }
+    bool left = g.solid(ax(q, axis, -1)), right = g.solid(q);
+    if (left != right) {
+      valid = true;
+      return 0.f;
+    }
+    if (left && right) {
+      float reflection;
+      if (!reflect(q, axis, reflection)) {
+        valid = false;
+        return 0.f;
+      }
+      parity *= reflection;
+    }
+    long long f = g.face_local(q, axis);
+    valid = vb[f] > .5f;
+    return parity * (forward ? D.fwd[f] : m.A[D.N + f]);
+  }
+  // sampled_component (coupled_motion.glslinc:112-137)
+  __device__ __noinline__ float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
+    const Grid& g = m.g;
+    const Dev& D = m.D;
+    F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);
+    lattice[axis] += .5f;
+    I3 lo = mk((int)floorf(lattice.x), (int)floorf(lattice.y), (int)floorf(lattice.z));
+    F3 t = mf(fract_(lattice.x), fract_(lattice.y), fract_(lattice.z));
+    lim0 = 1e20f;
+    lim1 = -1e20f;
+    valid = true;
+    bool interior = (D.flags & 8) != 0 && lo.x >= 1 && lo.y >= 1 && lo.z >= 1 && lo.x + 1 < D.nx && lo.y + 1 < D.ny &&
+                    lo.z + 1 < D.nz && !g.solid(mk(lo.x + 1, lo.y - 1, lo.z));
+    int fnx = D.nx + (axis == 0), fny = D.ny + (axis == 1);
+    float values[8];
+    for (int c = 0; c < 8; c++) {
+      int xx = c & 1, y = (c >> 1) & 1, z = c >> 2;
+      bool supported;
+      float value;
+      if (interior) {
+        long long base = g.face_local(lo, axis);
+        long long f = base + (long long)(xx + fnx * (y + fny * z));
+        supported = vb[f] > .5f;
+        value = forward ? D.fwd[f] : m.A[D.N + f];
+      } else
+        value = donor(addI(lo, mk(xx, y, z)), axis, forward, supported);
+      values[c] = value;
+      float wx = xx ? t.x : 1.f - t.x, wy = y ? t.y : 1.f - t.y, wz = z ? t.z : 1.f - t.z;
+      if (wx * wy * wz > 0.f) {
+        valid = valid && supported;
+        lim0 = mnf(lim0, value);
+        lim1 = mxf(lim1, value);
+      }
+    }
+    float a = __fmaf_rn(t.x, values[1] - values[0], values[0]), b = __fmaf_rn(t.x, values[3] - values[2], values[2]);
+    float d = __fmaf_rn(t.x, values[5] - values[4], values[4]), e = __fmaf_rn(t.x, values[7] - values[6], values[6]);
+    float lower = __fmaf_rn(t.y, b - a, a), upper = __fmaf_rn(t.y, e - d, d);
+    return __fmaf_rn(t.z, upper - lower, lower);
+  }
+  DI F3 velocity(F3 x) const {
+    F3 v;
+    bool valid;
+    float l0, l1v;
+    for (int axis = 0; axis < 3; axis++) v[axis] = sample(x, axis, false, valid, l0, l1v);
+    return v;
+  }
+  DI F3 velocity_checked(F3 x, bool& supported) const {
+    F3 v;
+    supported = true;
+    for (int axis = 0; axis < 3; axis++) {
+      bool valid;
+      float l0, l1v;
+      v[axis] = sample(x, axis, false, valid, l0, l1v);
+      supported = supported && valid;
+    }
+    return v;
+  }
+  DI float endpoint(F3 x, int component, bool forward, bool& supported, float& lim0, float& lim1) const {
+    float value = 0.f;
+    supported = true;
+    lim0 = 0.f;
+    lim1 = 0.f;
+    for (int axis = 0; axis < 3; axis++) {
+      bool valid;
+      float d0, d1;
+      float dv = sample(x, axis, axis == component && forward, valid, d0, d1);
+      supported = supported && valid;
+      if (axis == component) {
+        value = dv;
+        lim0 = d0;
+        lim1 = d1;
+      }
+    }
+    return value;
+  }
+  DI bool solid_at(F3 p) const {
+    const Dev& D = m.D;
+    return m.g.solid(mk((int)floorf(p.x / D.hx), (int)floorf(p.y / D.hy), (int)floorf(p.z / D.hz)));
+  }
+  DI F3 trace(F3 x, float d) const {
+    F3 s = velocity(x);
+    float hd = .5f * d;
+    F3 mid = mf(x.x - hd * s.x, x.y - hd * s.y, x.z - hd * s.z);
+    F3 s2 = velocity(mid);
+    return mf(x.x - d * s2.x, x.y - d * s2.y, x.z - d * s2.z);
+  }
+  DI bool trace_supported(F3 x, float d) const {
+    F3 s = velocity(x);
+    float hd = .5f * d;
+    F3 mid = mf(x.x - hd * s.x, x.y - hd * s.y, x.z - hd * s.z);
+    F3 s2 = velocity(mid);
+    F3 end = mf(x.x - d * s2.x, x.y - d * s2.y, x.z - d * s2.z);
+    for (int stage = 0; stage < 3; stage++) {
+      F3 p = stage == 0 ? x : (stage == 1 ? mid : end);
+      if (solid_at(p)) return false;
+      for (int axis = 0; axis < 3; axis++) {
+        bool valid;
+        float l0, l1v;
+        sample(p, axis, false, valid, l0, l1v);
+        if (!valid) return false;
+      }
+    }
+    return true;
+  }
+};
+
+// ---------------------------------------------------------------- op 27 / op 28
+// Face position of face (q, axis) in local coordinates (coupled_motion.glslinc:411).
+DI F3 face_x(const Dev& D, const Grid& g, I3 q, int axis) {
+  F3 x = mf(((float)q.x + .5f) * D.hx, ((float)q.y + .5f) * D.hy, ((float)q.z + .5f) * D.hz);
+  x[axis] -= .5f * g.h(axis);
+  return x;
+}
+// cached_advection, forward pass (coupled_motion.glslinc:170-179); dbg (optional) gets 16 floats.
+DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float* dbg) {
+  const Dev& D = mc.m.D;
+  long long nf = D.NF;
+  bool vs, vm, ve;
+  float l0, l1v;
+  F3 sv = mc.velocity_checked(x, vs);
+  float hd = .5f * d;
+  F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
+  F3 s2 = mc.velocity_checked(mid, vm);
+  F3 end = mf(x.x - d * s2.x, x.y - d * s2.y, x.z - d * s2.z);
+  float value = mc.endpoint(end, axis, false, ve, l0, l1v);
+  bool clear = !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end);
+  if (dbg) {
+    float t[16] = {x.x, x.y, x.z, sv.x, sv.y, sv.z, (float)vs, mid.x, mid.y, mid.z, (float)vm, end.x, end.y, end.z, (float)ve, (float)clear};
+    for (int k = 0; k < 16; k++) dbg[k] = t[k];
+    return value;
+  }
+  D.tcache[i] = l0;
+  D.tcache[nf + i] = l1v;
+  D.tcache[2 * nf + i] = (vs && vm && ve && clear) ? 1.f : 0.f;
+  D.tcache[3 * nf + i] = sv.x;
+  D.tcache[4 * nf + i] = sv.y;
+  D.tcache[5 * nf + i] = sv.z;
+  return value;
+}
+// cached_advection, corrected pass (coupled_motion.glslinc:180-187)
+DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
+  const Dev& D = mc.m.D;
+  long long nf = D.NF;
+  float forward = D.fwd[i];
+  if (D.tcache[2 * nf + i] < .5f) return forward;
+  F3 sv = mf(D.tcache[3 * nf + i], D.tcache[4 * nf + i], D.tcache[5 * nf + i]);
+  bool vm, ve;
+  float u0, u1;
+  float rd = -d;
+  float hd = .5f * rd;
+  F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
+  F3 s2 = mc.velocity_checked(mid, vm);
+  F3 end = mf(x.x - rd * s2.x, x.y - rd * s2.y, x.z - rd * s2.z);
+  float backward = mc.endpoint(end, axis, true, ve, u0, u1);
+  float corrected = forward + .5f * (mc.m.A[D.N + i] - backward);
+  return (vm && ve && !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end) && corrected >= D.tcache[i] &&
+          corrected <= D.tcache[nf + i])
+             ? corrected
+             : forward;
+}
+__global__ void __launch_bounds__(NT) k_mac(Dev D, int op) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  Mac mc(m);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.NF) return;
+  I3 q;
+  int axis;
+  m.g.unpack_face(i, q, axis);
+  F3 x = face_x(D, m.g, q, axis);
+  float value = 0.f;
+  float d = m.dt;
+  if (!m.g.wall_face(q, axis) && ((D.flags & 2) == 0 || mc.vb[i] > .5f)) {
+    if (D.flags & 4) {
+      if (op == 27) value = mac_forward(mc, x, axis, d, i, nullptr);
+      else value = mac_correct(mc, x, axis, d, i);
+    } else if (op == 27) {
+      bool valid;
+      float l0, l1v;
+      value = mc.sample(mc.trace(x, d), axis, false, valid, l0, l1v);
+    } else {
+      bool valid, vf;
+      float l0, l1v, d0, d1;
+      float backward = mc.sample(mc.trace(x, -d), axis, true, valid, l0, l1v);
+      mc.sample(mc.trace(x, d), axis, false, vf, d0, d1);
+      float forward = D.fwd[i], corrected = forward + .5f * (m.A[D.N + i] - backward);
+      value = (valid && vf && mc.trace_supported(x, d) && mc.trace_supported(x, -d) && corrected >= d0 && corrected <= d1)
+                  ? corrected
+                  : forward;
+    }
+  }
+  if (op == 27) D.fwd[i] = value;
+  else m.Cb[D.N + i] = value;
+}
+// Debug probe: the op-27 forward trace of one face (16 floats + value).
+__global__ void k_debug_face(Dev D, long long i, float* out) {
+  Motion m(D);
+  Mac mc(m);
+  I3 q;
+  int axis;
+  m.g.unpack_face(i, q, axis);
+  F3 x = face_x(D, m.g, q, axis);
+  out[16] = mac_forward(mc, x, axis, m.dt, i, out);
+  out[17] = (float)axis;
+  out[18] = (float)q.x;
+  out[19] = (float)q.y;
+}
+
+// Debug probe: one sampled component with its eight donors (include/waves_debug.h).
+__global__ void k_debug_sample(Dev D, float x, float y, float z, int axis, int forward, float* out) {
+  Motion m(D);
+  Mac mc(m);
+  bool valid;
+  float l0, l1;
+  F3 p = mf(x, y, z);
+  out[0] = mc.sample(p, axis, forward != 0, valid, l0, l1);
+  out[1] = valid;
+  out[2] = l0;
+  out[3] = l1;
+  F3 lattice = mf(p.x / D.hx - .5f, p.y / D.hy - .5f, p.z / D.hz - .5f);
+  lattice[axis] += .5f;
+  out[4] = lattice.x;
+  out[5] = lattice.y;
+  out[6] = lattice.z;
+  I3 lo = mk((int)floorf(lattice.x), (int)floorf(lattice.y), (int)floorf(lattice.z));
+  for (int c = 0; c < 8; c++) {
+    bool sup;
+    I3 q = addI(lo, mk(c & 1, (c >> 1) & 1, c >> 2));
+    out[8 + 4 * c] = mc.donor(q, axis, forward != 0, sup);
+    out[9 + 4 * c] = sup;
+    out[10 + 4 * c] = m.g.solid(q);
+    out[11 + 4 * c] = m.g.wall_face(q, axis);
+  }
+}
+
+}  // namespace
+
+static unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
+
+void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis, int forward, float* out) {
+  if (axis < 0) k_debug_face<<<1, 1, 0, s>>>(D, (long long)x[0], out);
+  else k_debug_sample<<<1, 1, 0, s>>>(D, x[0], x[1], x[2], axis, forward, out);
+}
+
+void launch_motion_cfl(const Dev& D, cudaStream_t s) {
+  k_cfl<<<grid_for(D.N), NT, 0, s>>>(D);
+  k_compress<<<grid_for(D.N), NT, 0, s>>>(D);
+}
+void launch_sweep(const Dev& D, cudaStream_t s) {
+  k_sweep_plane<<<grid_for(D.N), NT, 0, s>>>(D);
+  k_sweep_update<<<grid_for(D.N), NT, 0, s>>>(D);
+}
+void launch_maccormack(const Dev& D, cudaStream_t s) {
+  k_mac<<<grid_for(D.NF), NT, 0, s>>>(D, 27);
+  k_mac<<<grid_for(D.NF), NT, 0, s>>>(D, 28);
+}
+
+}  // namespace wg

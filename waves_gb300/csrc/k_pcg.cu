@@ -1,0 +1,194 @@
+// Preconditioned CG on the fine ghost-fluid operator
+// (neuron-forest/waves water/shaders/compute/pressure_iterations.glslinc ops 3-10).
+// Inner products, the residual norm and ||b||^2 are accumulated in FP64; vector updates stay FP32.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace wg {
+
+namespace {
+constexpr int NT = 256;
+
+// Fine 7-point operator applied to a vector that is zero off the wet set
+// (pressure_core.glslinc:119-125).
+DI float operator_at(const Dev& D, const Grid& g, I3 q, long long i, const float* x) {
+  float here = D.kind[i] > 0 ? x[i] : 0.f;
+  float result = 0.f;
+  int face = 0;
+  for (int axis = 0; axis < 3; axis++)
+    for (int sign = -1; sign <= 1; sign += 2) {
+      I3 nb = g.wrap_cell(ax(q, axis, sign));
+      float other = 0.f;
+      if (!g.outside(nb)) {
+        long long j = g.index3(nb);
+        if (D.kind[j] > 0) other = x[j];
+      }
+      float k = D.coef[(long long)face * D.N + i];
+      result += k * (here - other);
+      face++;
+    }
+  return result;
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------- op 3 (+ op 4 when the V-cycle is off)
+__global__ void __launch_bounds__(NT) k_cg_init(Dev D) {
+  if (!pressure_setup(D)) return;
+  Grid g(D);
+  const float* Cb = bank_ptr(D, 1 - acc_bank(D));
+  const float* p = Cb + D.N + D.NF;
+  float dt = (float)D.c[20];
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[4] = {0, 0, 0, 0};
+  if (i < D.N) {
+    I3 q = g.coord(i);
+    float r = 0.f, z = 0.f, bv = 0.f, diag = 1.f;
+    if (D.kind[i] > 0) {
+      diag = D.diag[i];
+      float dv = 0.f;
+      for (int axis = 0; axis < 3; axis++) {
+        I3 right = ax(q, axis, 1);
+        dv += (Cb[g.face_index(right, axis)] - Cb[g.face_index(q, axis)]) / g.h(axis);
+      }
+      bv = -1000.0f / dt * dv;
+      r = bv - operator_at(D, g, q, i, p);
+      z = r / diag;
+    }
+    D.r[i] = r;
+    D.z[i] = z;
+    D.d[i] = z;
+    D.diag[i] = diag;
+    D.b[i] = bv;
+    v[0] = (double)r * (double)z;
+    v[1] = (double)r * (double)r;
+    v[2] = (double)bv * (double)bv;
+    v[3] = (double)fabsf(r);
+  }
+  const int ops[4] = {0, 0, 0, 1};
+  double out[4];
+  if (last_block_reduce<NT, 4>(D, kSiteCGInit, v, ops, out) && threadIdx.x == 0) {
+    // The V-cycle (and its own op 4) runs exactly when no failure is latched.
+    if (D.c[7] > .5) finalize_op4(D, out);
+  }
+}
+
+// ---------------------------------------------------------------- op 5 + 6 + 7
+__global__ void __launch_bounds__(NT) k_cg_matvec(Dev D) {
+  if (!solving(D)) return;
+  Grid g(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[1] = {0};
+  if (i < D.N) {
+    float qv = D.kind[i] > 0 ? operator_at(D, g, g.coord(i), i, D.d) : 0.f;
+    D.q[i] = qv;
+    v[0] = (double)D.d[i] * (double)qv;
+  }
+  const int ops[1] = {0};
+  double out[1];
+  if (last_block_reduce<NT, 1>(D, kSiteDot, v, ops, out) && threadIdx.x == 0) {
+    double dotp = out[0];
+    if (dotp <= 0 || isnan(dotp) || isinf(dotp)) D.c[7] = 1;
+    else D.c[11] = D.c[9] / dotp;
+  }
+}
+
+// ---------------------------------------------------------------- op 8 + multigrid load (op 5 of the cycle)
+template <class T> __global__ void __launch_bounds__(NT) k_cg_update(Dev D) {
+  if (!solving(D)) return;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  float a = (float)D.c[11];
+  float* p = bank_ptr(D, 1 - acc_bank(D)) + D.N + D.NF;
+  float r = D.r[i] - a * D.q[i];
+  p[i] = p[i] + a * D.d[i];
+  D.r[i] = r;
+  T* v = (T*)D.mgv;
+  long long M = D.mg_nodes;
+  v[i] = st_val<T>(r);      // field 0 rhs
+  v[M + i] = st_val<T>(0.f);  // field 1
+  v[2 * M + i] = st_val<T>(0.f);  // field 2
+}
+
+// ---------------------------------------------------------------- op 10 (+ loop condition)
+__global__ void __launch_bounds__(NT) k_cg_direction(Dev D, cudaGraphConditionalHandle h, int use_handle) {
+  bool on = solving(D);
+  if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) {
+    // The body has run ops 5-10 of one iteration; continue while solving.
+    cudaGraphSetConditional(h, on ? 1u : 0u);
+  }
+  if (!on) return;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  float b = (float)D.c[12];
+  D.d[i] = D.z[i] + b * D.d[i];
+}
+
+// ---------------------------------------------------------------- graph conditions
+__global__ void k_set_cond(Dev D, cudaGraphConditionalHandle h, int which) {
+  const double* c = D.c;
+  bool v;
+  if (which == kCondDefectFirst) v = true;
+  else if (which == kCondActive) v = c[4] > .5;
+  else if (which == kCondSolving) v = c[4] > 0.5 && c[6] < 0.5 && c[7] < 0.5;
+  else v = c[57] == 1 && c[7] < .5 && c[4] > .5;
+  cudaGraphSetConditional(h, v ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------- ops 43 + 1 (trial begin) and 63/64
+__global__ void k_begin(Dev D) {
+  double* c = D.c;
+  // op 43 (coupled_motion.glslinc:351-355)
+  bool retry = c[7] == 20 || (c[7] >= 10 && c[7] <= 12);
+  if (retry && c[29] < 2) {
+    c[33] = c[7]; c[34] = c[20]; c[30] = c[20] * .5; c[29] += 1; c[7] = 0; c[4] = 0; c[5] = 0;
+  }
+  // op 1 (pressure_pass.glslinc:199-203)
+  c[5] = 0;
+  double quota = c[kQuota];
+  if (c[7] > 0.5 || (quota >= 0 ? c[2] >= quota : c[1] >= -quota)) return;
+  if (c[4] < 0.5) {
+    c[4] = 1; c[5] = 1; c[6] = 0; c[8] = 0; c[13] = 1;
+    c[32] += 1; c[57] = 0; c[58] = 0;
+  }
+}
+__global__ void __launch_bounds__(NT) k_defect_begin(Dev D) {
+  const double* c = D.c;
+  double c57 = c[57];
+  bool go = (c57 == 1 || c57 == 2) && c[7] < .5;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (!go) return;
+  if (i == 0 && c57 == 1) {  // op 1 of the next batch (pending: setup off), then op 63
+    D.c[5] = 0;
+    D.c[57] = 2;
+    D.c[6] = 0;
+    D.c[8] = 0;
+  }
+  if (i >= D.N) return;  // op 64
+  float* p = bank_ptr(D, 1 - acc_bank(D)) + D.N + D.NF;
+  D.pbase[i] = p[i];
+  p[i] = 0.f;
+}
+
+}  // namespace
+
+static unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
+
+void launch_begin(const Dev& D, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(D); }
+void launch_defect_begin(const Dev& D, cudaStream_t s) { k_defect_begin<<<grid_for(D.N), NT, 0, s>>>(D); }
+void launch_cg_init(const Dev& D, cudaStream_t s) { k_cg_init<<<grid_for(D.N), NT, 0, s>>>(D); }
+void launch_cg_matvec(const Dev& D, cudaStream_t s) { k_cg_matvec<<<grid_for(D.N), NT, 0, s>>>(D); }
+void launch_cg_update(const Dev& D, cudaStream_t s) {
+  if (D.bf16) k_cg_update<__nv_bfloat16><<<grid_for(D.N), NT, 0, s>>>(D);
+  else k_cg_update<float><<<grid_for(D.N), NT, 0, s>>>(D);
+}
+void launch_cg_direction(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int use_handle) {
+  k_cg_direction<<<grid_for(D.N), NT, 0, s>>>(D, h, use_handle);
+}
+void launch_set_cond(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int which) {
+  k_set_cond<<<1, 1, 0, s>>>(D, h, which);
+}
+
+}  // namespace wg
