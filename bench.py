@@ -1,0 +1,295 @@
+#!/usr/bin/env python
+"""Benchmark of the waves solver step: simulated seconds per wall second on the 310x48x80 beach.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mg 32|16]
+
+A "step" is one accepted solver step (CFL, three VOF sweeps, MacCormack, offshore forcing,
+geometry, multigrid build, MGPCG to relative residual 1e-6, extension, acceptance; retries and
+defect corrections included).  The state is resident in HBM; the device time of each trial comes
+from CUDA events the library records on its own stream.  L2 is flushed (a 256 MiB write) between
+timed steps.  `value` = simulated seconds advanced / device seconds.  `e2e` drives the same
+solver frame by frame through the C ABI with host buffers: request_time, run, the telemetry
+read-back and the accepted-surface export to host memory, timed with the host clock.
+
+--impl reference times the CPU restatement of the reference's algorithm (the oracle, all host
+threads) on the same configuration and prints the same line with "impl": "reference".
+With torchrun (N > 1) every rank runs an independent replica of the beach (the solver step has
+no data-parallel exchange; replicas only); value = total simulated seconds / max wall over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sim-s per wall-s at 310x48x80; pressure ms/step, learned+BF16 vs plain FP32"
+UNIT = "sim-s/wall-s"
+TOL = 1e-6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=240)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mg", type=int, default=32, choices=[32, 16])
+    ap.add_argument("--e2e-frames", type=int, default=30)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5).stdout
+                for line in out.strip().splitlines():
+                    self.rows.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=6)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 4 + k and r[4 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def beach_config(mg):
+    import waves_gb300 as wg
+    return wg.config("beach", pressure_tolerance=TOL, mg_precision=mg)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import waves_gb300 as wg
+    from waves_gb300.build import build
+    if rank == 0:
+        build()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.set_device(local)
+    cfg = beach_config(args.mg)
+    cfg.device = local
+    s = wg.WavesSolver(cfg)
+    lib, h = s.lib, s.h
+    import ctypes as C
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def timing(reset):
+        m, p, t = C.c_double(), C.c_double(), C.c_int64()
+        s._ck(lib.waves_timing(h, C.byref(m), C.byref(p), C.byref(t), reset))
+        return m.value, p.value, t.value
+
+    def one_step():
+        c = s.control()
+        target = int(c[2]) + 1
+        s.request_steps(target)
+        while True:
+            s.advance(1)
+            c = s.control()
+            if c[2] >= target:
+                return c
+            if c[7] > .5 and not ((c[7] == 20 or 10 <= c[7] <= 12) and c[29] < 2):
+                raise RuntimeError(f"solver halted with code {c[7]}")
+
+    for _ in range(max(args.warmup, 3)):
+        one_step()
+    timing(True)
+    c0 = s.control()
+    stats0 = s.stats()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    motion = pressure = 0.0
+    with Clocks(local) as clk:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            one_step()
+        wall = time.perf_counter() - wall0
+    torch.cuda.synchronize()
+    motion, pressure, trials = timing(True)
+    c1 = s.control()
+    sim = c1[1] - c0[1]
+    dev_s = (motion + pressure) / 1e3
+    counts = (C.c_int32 * 8)()
+    lib.waves_debug_launch_counts(h, counts)
+    counts = list(counts)
+    active = c1[32] - c0[32]
+    rounds = active + (c1[103] - c0[103])
+    iters = c1[18] - c0[18]
+    # per trial: begin + condition, and when active: motion, pressure set-up, conditions, trial end;
+    # per defect round: CG set-up + conditions + post; per CG iteration: the iteration kernels
+    launches = int(trials * (counts[0] + counts[7] * 2) + active * (counts[1] + counts[2] + counts[6] + counts[7])
+                   + rounds * (counts[3] + counts[5] + 2 * counts[7]) + iters * counts[4])
+    out = {
+        "sim_s": sim, "device_s": dev_s, "wall_s": wall, "steps": int(c1[2] - c0[2]), "trials": trials,
+        "motion_ms": motion, "pressure_ms": pressure, "iters": iters, "defect_rounds": rounds - active,
+        "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
+        "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
+    }
+    # e2e: frames through the public API with host buffers
+    e2e = None
+    if args.e2e_frames > 0:
+        planes = np.empty(4 * s.N, dtype=np.float32)
+        kinds = np.empty(s.N, dtype=np.float32)
+        t_sim0 = s.control()[1]
+        w0 = time.perf_counter()
+        for f in range(args.e2e_frames):
+            s.request_time(t_sim0 + (f + 1) / 60.0)
+            s.run(4)
+            st = s.stats()
+            lib.waves_export_surface(h, planes.ctypes.data_as(C.POINTER(C.c_float)), kinds.ctypes.data_as(C.POINTER(C.c_float)))
+        w = time.perf_counter() - w0
+        sim_e = s.control()[1] - t_sim0
+        e2e = {"sim_s": sim_e, "wall_s": w, "frames": args.e2e_frames,
+               "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8)}
+    out["e2e"] = e2e
+    s.close()
+    return out
+
+
+def cpu_baseline(args, cfg_mg, seconds):
+    """The oracle (CPU restatement, FP32, all host threads) on the beach for a bounded sample."""
+    from tests.oracle_ref import Oracle
+    cfg = beach_config(cfg_mg)
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    o = Oracle(cfg, 32)
+    t0 = time.perf_counter()
+    steps = 0
+    while time.perf_counter() - t0 < seconds or steps == 0:
+        steps += 1
+        o.request_steps(steps)
+        o.run()
+    wall = time.perf_counter() - t0
+    c = o.control()
+    return {"value": c[1] / wall, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)),
+            "kind": "port", "sample": f"{steps} accepted steps of the 310x48x80 beach from rest ({c[1]:.4f} sim-s, {wall:.1f} s)"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base = cpu_baseline(args, args.mg, max(args.cpu_seconds, 1.0))
+        line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "beach 310x48x80 (lab_runner.gd settings), plain FP32 MGPCG, tol 1e-6",
+                           "cells": 1190400},
+                "impl": "reference",
+                "cpu_baseline": {"value": base["value"], "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
+                                 "sample": base["sample"]},
+                "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    res = run_ours(args, world, rank, local)
+    sim, dev = res["sim_s"], res["device_s"]
+    if world > 1:
+        t = torch.tensor([sim, dev, res["e2e"]["sim_s"] if res["e2e"] else 0.0], dtype=torch.float64, device=f"cuda:{local}")
+        mx = torch.tensor([dev, res["e2e"]["wall_s"] if res["e2e"] else 0.0], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sim_total, dev_max, e2e_sim, e2e_wall = t[0].item(), mx[0].item(), t[2].item(), mx[1].item()
+    else:
+        sim_total, dev_max = sim, dev
+        e2e_sim = res["e2e"]["sim_s"] if res["e2e"] else 0.0
+        e2e_wall = res["e2e"]["wall_s"] if res["e2e"] else 0.0
+    if rank != 0:
+        torch.distributed.destroy_process_group() if world > 1 else None
+        return
+    steps = max(res["steps"], 1)
+    line = {
+        "metric": METRIC,
+        "value": sim_total / dev_max,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_max * 1e3 / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32" if args.mg == 32 else "f32+bf16mg",
+        "data": "synthetic",
+        "config": {"workload": "beach 310x48x80 (lab_runner.gd settings), "
+                               + ("plain FP32 MGPCG" if args.mg == 32 else "BF16 multigrid, FP32 CG") + ", tol 1e-6",
+                   "cells": 1190400, "l2": "flushed between steps (256 MiB write)",
+                   "sim_window_s": [res["t_end"] - res["sim_s"], res["t_end"]],
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "pressure_ms_per_step": res["pressure_ms"] / steps,
+        "motion_ms_per_step": res["motion_ms"] / steps,
+        "cg_iterations_per_step": res["iters"] / steps,
+        "defect_rounds": res["defect_rounds"],
+        "mg_builds": res["mg_builds"],
+        "trials": res["trials"],
+        "clocks": res["clocks"],
+        "gpu_launches": res["launches"],
+    }
+    if res["e2e"]:
+        e = res["e2e"]
+        line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"], "step": "one 1/60 s frame: request_time, run, stats, surface export"}
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            base = cpu_baseline(args, args.mg, args.cpu_seconds)
+            line["cpu_baseline"] = base
+        except Exception as ex:  # the oracle needs a C++ toolchain on the host
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(ex)[:200]}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

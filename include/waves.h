@@ -174,6 +174,13 @@ waves_status waves_advance(waves_handle* h, int32_t max_trials);
 waves_status waves_run(waves_handle* h, int32_t trials_per_sync);
 /* Wait for the handle's stream. */
 waves_status waves_synchronize(waves_handle* h);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own work after the
+ * solver's.  Every enqueue of this library goes to this stream. */
+void* waves_stream(waves_handle* h);
+/* Device time of the trials submitted so far, from CUDA events recorded on the handle's stream
+ * around each trial: the motion part (CFL, VOF, MacCormack, forcing) and the pressure part
+ * (geometry through acceptance, i.e. ops 17..13 of the reference).  Synchronises. */
+waves_status waves_timing(waves_handle* h, double* motion_ms, double* pressure_ms, int64_t* trials, int32_t reset);
 
 /* Telemetry snapshot (synchronises with the stream). */
 waves_status waves_stats(waves_handle* h, waves_stats_t* out);

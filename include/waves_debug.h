@@ -18,6 +18,9 @@ waves_status waves_debug_phase(waves_handle* h, int32_t phase);
 /* One MacCormack sampled component at local position x (40 floats: value, valid, limits, lattice,
  * then per donor: value, supported, solid, wall). */
 waves_status waves_debug_sample(waves_handle* h, const float* x, int32_t axis, int32_t forward, float* out40);
+/* Kernel launches per phase: begin, motion, pressure set-up, CG round set-up, CG iteration,
+ * projection/extension/acceptance, trial end, condition kernel. */
+waves_status waves_debug_launch_counts(waves_handle* h, int32_t* out8);
 waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size_t bytes);
 #ifdef __cplusplus
 }

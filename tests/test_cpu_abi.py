@@ -1,0 +1,48 @@
+"""The C-ABI library loads and exports every function that include/*.h declares (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import waves_gb300
+from waves_gb300.abi import WAVES_ABI_SYMBOLS
+from waves_gb300.build import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(waves_\w+)\s*\(", text))
+
+
+def test_library_exports_every_declared_symbol():
+    lib_path = build()
+    lib = ctypes.CDLL(lib_path)
+    names = declared("waves.h") | declared("waves_debug.h")
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_symbol_list_matches_header():
+    assert set(WAVES_ABI_SYMBOLS) == declared("waves.h")
+
+
+def test_presets_without_gpu():
+    lib = waves_gebuild = waves_gb300.load(build_if_missing=True)
+    beach = waves_gb300.config("beach")
+    assert tuple(beach.n) == (310, 48, 80)
+    assert abs(beach.wave[1] - 2.52502) < 1e-4  # lab_runner.gd:19-25 dispersion, T = 1.4 s, h = 0.45 m
+    tank = waves_gb300.config("tank")
+    assert tank.coastal == 0 and abs(tank.cfl - 0.5) < 1e-7 and abs(tank.pressure_tolerance - 1e-6) < 1e-12
+    assert abs(lib.waves_dispersion_k(1.4, 0.45) - 2.525) < 1e-3
+
+
+def test_create_without_device_fails_cleanly(monkeypatch):
+    # No GPU in this container: waves_create must report an error, not crash or fall back.
+    import torch
+    if torch.cuda.is_available():
+        return
+    import pytest
+    with pytest.raises(waves_gb300.WavesError):
+        waves_gb300.WavesSolver(waves_gb300.config("tank"))

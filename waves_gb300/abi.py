@@ -144,6 +144,8 @@ WAVES_ABI_SYMBOLS = [
     "waves_advance",
     "waves_run",
     "waves_synchronize",
+    "waves_stream",
+    "waves_timing",
     "waves_stats",
     "waves_control",
     "waves_set_control",
@@ -179,6 +181,8 @@ def declare(lib):
         "waves_advance": (C.c_int, [h, C.c_int32]),
         "waves_run": (C.c_int, [h, C.c_int32]),
         "waves_synchronize": (C.c_int, [h]),
+        "waves_stream": (C.c_void_p, [h]),
+        "waves_timing": (C.c_int, [h, P(C.c_double), P(C.c_double), P(C.c_int64), C.c_int32]),
         "waves_stats": (C.c_int, [h, P(WavesStats)]),
         "waves_control": (C.c_int, [h, P(C.c_double), C.c_int32]),
         "waves_set_control": (C.c_int, [h, P(C.c_double), C.c_int32]),
@@ -197,6 +201,7 @@ def declare(lib):
     }
     sig["waves_debug_phase"] = (C.c_int, [h, C.c_int32])
     sig["waves_debug_sample"] = (C.c_int, [h, P(C.c_float), C.c_int32, C.c_int32, P(C.c_float)])
+    sig["waves_debug_launch_counts"] = (C.c_int, [h, P(C.c_int32)])
     sig["waves_debug_read"] = (C.c_int, [h, C.c_char_p, C.c_void_p, C.c_size_t])
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

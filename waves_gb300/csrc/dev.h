@@ -19,6 +19,7 @@ enum CtrlExtra {
   kConservation = 100,  // V_now - V0 - sum of ledgers at the last acceptance
   kQuota = 101,         // request quota (>= 0 steps, < 0 minus a deadline)
   kWarmUsed = 102,      // trials started from the learned warm start
+  kDefectRounds = 103,  // defect-correction rounds run since creation
 };
 
 struct MGLevelDev {

@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(NT) k_defect_begin(Dev D) {
   if (!go) return;
   if (i == 0 && c57 == 1) {  // op 1 of the next batch (pending: setup off), then op 63
     D.c[5] = 0;
+    D.c[kDefectRounds] += 1;
     D.c[57] = 2;
     D.c[6] = 0;
     D.c[8] = 0;

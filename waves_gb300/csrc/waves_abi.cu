@@ -10,6 +10,7 @@
 //   * run from the host, reading the control block between phases (the debugging path).
 // Both paths enqueue the same kernels; results are identical.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -58,10 +59,17 @@ struct waves_handle {
   double* host_c = nullptr;  // pinned
   double* host_quota = nullptr;  // pinned
   std::atomic<double> quota{0.0};
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr, graph_p = nullptr;
+  cudaGraphExec_t exec = nullptr, exec_p = nullptr;  // motion part, pressure part
   bool graph_mode = true;
   std::string err;
+  // device timing of submitted trials: events (before motion, between, after pressure)
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::array<cudaEvent_t, 3>> ev_pending;
+  double motion_ms = 0, pressure_ms = 0;
+  int64_t timed_trials = 0;
+  // kernels per phase: begin, setup-motion, setup-pressure, cg round set-up, cg iteration, post, end
+  int32_t launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -363,15 +371,24 @@ waves_status setup_device(waves_handle* h) {
 }
 
 // ---------------------------------------------------------------- step enqueue
-void enqueue_setup(waves_handle* h, cudaStream_t s) {
+// Motion part of the set-up: CFL, VOF sweeps, MacCormack, coastal forcing.
+void enqueue_motion(waves_handle* h, cudaStream_t s) {
   const Dev& D = h->D;
   wg::launch_motion_cfl(D, s);
   for (int sweep = 0; sweep < 3; sweep++) wg::launch_sweep(D, s);
   wg::launch_maccormack(D, s);
   if (D.coastal) wg::launch_coastal(D, s);
+}
+// Pressure set-up: geometry, coefficients, projection set-up, multigrid build.
+void enqueue_pressure_setup(waves_handle* h, cudaStream_t s) {
+  const Dev& D = h->D;
   wg::launch_geometry(D, s);
   wg::launch_proj_setup(D, s);
   wg::launch_mg_build(D, s);
+}
+void enqueue_setup(waves_handle* h, cudaStream_t s) {
+  enqueue_motion(h, s);
+  enqueue_pressure_setup(h, s);
 }
 void enqueue_cg_begin(waves_handle* h, cudaStream_t s) {
   const Dev& D = h->D;
@@ -411,24 +428,69 @@ waves_status add_conditional(waves_handle* h, cudaStream_t s, cudaGraphCondition
   return WAVES_OK;
 }
 
+// Kernel nodes enqueued by `fn` (captured into a scratch graph and counted).
+template <class Fn> int32_t count_kernels(waves_handle* h, Fn fn) {
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return -1;
+  cudaGraph_t g = nullptr;
+  int32_t n = -1;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    fn(s);
+    if (cudaStreamEndCapture(s, &g) == cudaSuccess) {
+      size_t count = 0;
+      cudaGraphGetNodes(g, nullptr, &count);
+      n = (int32_t)count;
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaStreamDestroy(s);
+  cudaGetLastError();
+  return n;
+}
+void count_launches(waves_handle* h) {
+  const Dev& D = h->D;
+  h->launches[0] = count_kernels(h, [&](cudaStream_t s) { wg::launch_begin(D, s); });
+  h->launches[1] = count_kernels(h, [&](cudaStream_t s) { enqueue_motion(h, s); });
+  h->launches[2] = count_kernels(h, [&](cudaStream_t s) { enqueue_pressure_setup(h, s); });
+  h->launches[3] = count_kernels(h, [&](cudaStream_t s) { enqueue_cg_begin(h, s); });
+  h->launches[4] = count_kernels(h, [&](cudaStream_t s) { enqueue_cg_iteration(h, s, 0, 0); });
+  h->launches[5] = count_kernels(h, [&](cudaStream_t s) { wg::launch_post(D, s); });
+  h->launches[6] = count_kernels(h, [&](cudaStream_t s) { wg::launch_trial_end(D, s); });
+  h->launches[7] = 1;  // condition-setting kernel
+}
+
+// Motion graph: begin (ops 43, 1) and, if a trial is active, CFL/VOF/MacCormack/forcing.
+// Pressure graph: if active, geometry .. multigrid build, then WHILE(defect round) { CG set-up,
+// WHILE(solving) { CG iteration }, projection/extension/acceptance }, trial end.
 waves_status build_graph(waves_handle* h) {
   cudaStream_t s0 = h->stream, s1 = nullptr, s2 = nullptr, s3 = nullptr;
   CK(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking));
   waves_status st = WAVES_OK;
-  cudaGraph_t graph = nullptr;
   do {
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle hc;
+    cudaGraph_t body;
+    // --- motion graph
     CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
     wg::launch_begin(h->D, s0);
+    if ((st = add_conditional(h, s0, cudaGraphCondTypeIf, wg::kCondActive, &hc, &body)) != WAVES_OK) break;
+    CK(cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    enqueue_motion(h, s1);
+    CK(cudaStreamEndCapture(s1, &body));
+    CK(cudaStreamEndCapture(s0, &graph));
+    CK(cudaGraphInstantiate(&h->exec, graph, 0));
+    h->graph = graph;
+    // --- pressure graph
+    graph = nullptr;
     cudaGraphConditionalHandle h_active, h_defect, h_cg;
     cudaGraph_t body_active, body_defect, body_cg;
+    CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
     if ((st = add_conditional(h, s0, cudaGraphCondTypeIf, wg::kCondActive, &h_active, &body_active)) != WAVES_OK) break;
-    // --- trial body
     CK(cudaStreamBeginCaptureToGraph(s1, body_active, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    enqueue_setup(h, s1);
+    enqueue_pressure_setup(h, s1);
     if ((st = add_conditional(h, s1, cudaGraphCondTypeWhile, wg::kCondDefectFirst, &h_defect, &body_defect)) != WAVES_OK) break;
-    // --- defect-correction round
     CK(cudaStreamBeginCaptureToGraph(s2, body_defect, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     enqueue_cg_begin(h, s2);
     if ((st = add_conditional(h, s2, cudaGraphCondTypeWhile, wg::kCondSolving, &h_cg, &body_cg)) != WAVES_OK) break;
@@ -441,8 +503,8 @@ waves_status build_graph(waves_handle* h) {
     wg::launch_trial_end(h->D, s1);
     CK(cudaStreamEndCapture(s1, &body_active));
     CK(cudaStreamEndCapture(s0, &graph));
-    CK(cudaGraphInstantiate(&h->exec, graph, 0));
-    h->graph = graph;
+    CK(cudaGraphInstantiate(&h->exec_p, graph, 0));
+    h->graph_p = graph;
   } while (0);
   cudaStreamDestroy(s1);
   cudaStreamDestroy(s2);
@@ -450,7 +512,7 @@ waves_status build_graph(waves_handle* h) {
   if (st != WAVES_OK) {
     cudaStreamCaptureStatus cs;
     if (cudaStreamIsCapturing(s0, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-      cudaGraph_t junk;
+      cudaGraph_t junk = nullptr;
       cudaStreamEndCapture(s0, &junk);
       if (junk) cudaGraphDestroy(junk);
     }
@@ -459,9 +521,35 @@ waves_status build_graph(waves_handle* h) {
   return st;
 }
 
+cudaEvent_t take_event(waves_handle* h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+// Fold completed trial timings into the totals (called after a stream synchronisation).
+void collect_timing(waves_handle* h) {
+  for (auto& t : h->ev_pending) {
+    float a = 0, b = 0;
+    if (cudaEventElapsedTime(&a, t[0], t[1]) == cudaSuccess && cudaEventElapsedTime(&b, t[1], t[2]) == cudaSuccess) {
+      h->motion_ms += a;
+      h->pressure_ms += b;
+      h->timed_trials++;
+    }
+    for (cudaEvent_t e : t) h->ev_pool.push_back(e);
+  }
+  h->ev_pending.clear();
+  cudaGetLastError();
+}
+
 waves_status read_control(waves_handle* h) {
   CK(cudaMemcpyAsync(h->host_c, h->D.c, WAVES_CONTROL_SIZE * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  collect_timing(h);
   return WAVES_OK;
 }
 waves_status upload_quota(waves_handle* h) {
@@ -559,6 +647,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
     h->err = "initial commands failed";
     return fail(WAVES_CUDA_ERROR);
   }
+  count_launches(h);
   const char* mode = getenv("WAVES_SCHEDULE");
   h->graph_mode = !(mode && std::strcmp(mode, "host") == 0);
   if (h->graph_mode && build_graph(h) != WAVES_OK) {
@@ -576,6 +665,11 @@ void waves_destroy(waves_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
+  if (h->exec_p) cudaGraphExecDestroy(h->exec_p);
+  if (h->graph_p) cudaGraphDestroy(h->graph_p);
+  for (auto& t : h->ev_pending)
+    for (cudaEvent_t e : t) h->ev_pool.push_back(e);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (auto it = h->allocs.rbegin(); it != h->allocs.rend(); ++it) cudaFree(it->ptr);
   if (h->export_planes) cudaFree(h->export_planes);
   if (h->export_kinds) cudaFree(h->export_kinds);
@@ -603,7 +697,13 @@ waves_status waves_advance(waves_handle* h, int32_t max_trials) {
   if ((st = upload_quota(h)) != WAVES_OK) return st;
   for (int t = 0; t < max_trials; t++) {
     if (h->graph_mode) {
+      std::array<cudaEvent_t, 3> ev = {take_event(h), take_event(h), take_event(h)};
+      CK(cudaEventRecord(ev[0], h->stream));
       CK(cudaGraphLaunch(h->exec, h->stream));
+      CK(cudaEventRecord(ev[1], h->stream));
+      CK(cudaGraphLaunch(h->exec_p, h->stream));
+      CK(cudaEventRecord(ev[2], h->stream));
+      h->ev_pending.push_back(ev);
     } else if ((st = host_trial(h)) != WAVES_OK)
       return st;
   }
@@ -614,6 +714,23 @@ waves_status waves_synchronize(waves_handle* h) {
   if (!h) return WAVES_INVALID_ARG;
   CK(cudaStreamSynchronize(h->stream));
   CK(cudaGetLastError());
+  collect_timing(h);
+  return WAVES_OK;
+}
+
+void* waves_stream(waves_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+waves_status waves_timing(waves_handle* h, double* motion_ms, double* pressure_ms, int64_t* trials, int32_t reset) {
+  if (!h) return WAVES_INVALID_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  collect_timing(h);
+  if (motion_ms) *motion_ms = h->motion_ms;
+  if (pressure_ms) *pressure_ms = h->pressure_ms;
+  if (trials) *trials = h->timed_trials;
+  if (reset) {
+    h->motion_ms = h->pressure_ms = 0;
+    h->timed_trials = 0;
+  }
   return WAVES_OK;
 }
 
@@ -874,6 +991,11 @@ waves_status waves_debug_sample(waves_handle* h, const float* x, int32_t axis, i
   CK(cudaStreamSynchronize(h->stream));
   CK(cudaMemcpy(out40, d, 40 * sizeof(float), cudaMemcpyDeviceToHost));
   cudaFree(d);
+  return WAVES_OK;
+}
+waves_status waves_debug_launch_counts(waves_handle* h, int32_t* out8) {
+  if (!h || !out8) return WAVES_INVALID_ARG;
+  std::memcpy(out8, h->launches, sizeof(h->launches));
   return WAVES_OK;
 }
 waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size_t bytes) {
