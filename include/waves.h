@@ -226,6 +226,18 @@ typedef struct waves_warm_start_model {
 } waves_warm_start_model;
 waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model* model);
 
+/* Liquid volume sum over cells of F * hx*hy*hz (FP64) of a caller-owned device array F[nx*ny*nz]
+ * (x-fastest), written to the caller-owned device double *out, enqueued on `stream` (a
+ * cudaStream_t; NULL = default stream).  No counterpart in the reference.  It allocates nothing:
+ * for hosts that cannot let the library call cudaMalloc (engine-owned GPU memory, no allocation
+ * inside a frame); its scratch is a fixed 64 KiB device array in the library, so it accepts at most
+ * 2,097,152 cells (WAVES_INVALID_ARG beyond).  The first call on a device resolves that array's
+ * address for the current device; make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  Bit-identical to waves_stats().initial_volume_m3 for the
+ * solver's initial F. */
+waves_status waves_liquid_volume_noalloc(const float* F, int32_t nx, int32_t ny, int32_t nz, float hx, float hy, float hz,
+                                         double* out, void* stream);
+
 /* Last error text of this handle (or of the last failed waves_create when h is NULL). */
 const char* waves_last_error(const waves_handle* h);
 

@@ -161,6 +161,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_load",
     "waves_set_warm_start",
     "waves_last_error",
+    "waves_liquid_volume_noalloc",
 ]
 
 
@@ -198,6 +199,8 @@ def declare(lib):
         "waves_load": (C.c_int, [h, C.c_void_p, C.c_size_t]),
         "waves_set_warm_start": (C.c_int, [h, P(WavesWarmStartModel)]),
         "waves_last_error": (C.c_char_p, [h]),
+        "waves_liquid_volume_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float,
+                                                  C.c_float, C.c_void_p, C.c_void_p]),
     }
     sig["waves_debug_phase"] = (C.c_int, [h, C.c_int32])
     sig["waves_debug_sample"] = (C.c_int, [h, P(C.c_float), C.c_int32, C.c_int32, P(C.c_float)])
