@@ -22,5 +22,20 @@ def beach_slope(**kw):
     return wg.config("beach", n=(64, 40, 8), origin=(0.5, -0.6, -0.2), **kw)
 
 
+def beach_slope_bf16(**kw):
+    """beach_slope with the BF16 multigrid (storage and smoothing in BF16, FP32 arithmetic)."""
+    return beach_slope(mg_precision=16, **kw)
+
+
+def tank_bf16(**kw):
+    return tank_small(mg_precision=16, **kw)
+
+
+def tank_jacobi(**kw):
+    """Jacobi smoothing, rebuild-every-trial maintenance: the other multigrid options."""
+    return tank_small(mg_smoother=0, mg_smoothing=2, mg_maintenance=0, **kw)
+
+
 CASES = {"tank_small": tank_small, "tank_ref_cfl": tank_ref_cfl, "beach_coarse": beach_coarse,
-         "beach_slope": beach_slope}
+         "beach_slope": beach_slope, "beach_slope_bf16": beach_slope_bf16, "tank_bf16": tank_bf16,
+         "tank_jacobi": tank_jacobi}

@@ -57,7 +57,12 @@ DI float tcosh(float x) { return (float)cosh((double)x); }
 DI float texp(float x) { return (float)exp((double)x); }
 DI float tpow4(float x) { double d = (double)x; return (float)(d * d * d * d); }
 // periodic_index.glslinc:3-6
-DI int pidx(int q, int n) { return q >= 0 ? q % n : n - 1 - ((-1 - q) % n); }
+DI int pidx(int q, int n) {
+  if (q >= 0 && q < n) return q;
+  if (q < 0 && q >= -n) return q + n;
+  if (q >= n && q < 2 * n) return q - n;
+  return q >= 0 ? q % n : n - 1 - ((-1 - q) % n);
+}
 
 // ---------------------------------------------------------------- grid helpers
 struct Grid {
@@ -121,6 +126,12 @@ struct Grid {
     return D.NU + D.NV + (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)D.ny * q.z);
   }
   DI long long face_index(I3 q, int axis) const { return D.N + face_local(q, axis); }
+  // lattice index of face (q, axis) without folding periodic duplicates
+  DI long long face_local_raw(I3 q, int axis) const {
+    if (axis == 0) return (long long)q.x + (long long)(D.nx + 1) * ((long long)q.y + (long long)D.ny * q.z);
+    if (axis == 1) return D.NU + (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)(D.ny + 1) * q.z);
+    return D.NU + D.NV + (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)D.ny * q.z);
+  }
   DI void unpack_face(long long f, I3& q, int& axis) const {
     long long base;
     int mx_, my_;
@@ -358,11 +369,12 @@ template <int NT, int K>
 DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (&ops)[K], double (&out)[K]) {
   __shared__ double sh[32];
   __shared__ bool am_last;
-  const int nb = gridDim.x;
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   double* part = D.part;
   for (int k = 0; k < K; k++) {
     double r = ops[k] == 0 ? block_reduce<NT>(vals[k], AddD(), sh) : block_reduce<NT>(vals[k], MaxD(), sh);
-    if (threadIdx.x == 0) part[(size_t)k * nb + blockIdx.x] = r;
+    if (threadIdx.x == 0) part[(size_t)k * nb + bid] = r;
   }
   __threadfence();
   __syncthreads();

@@ -32,6 +32,8 @@ struct MGLevelDev {
   long long eoff;    // offset of this level's ELL values
   long long toff;    // offset of this level's transfer cache
   int soff;          // offset of this level's stencil in the stencil table
+  int roff[3];       // restriction tables of this (coarse) level, per axis (4 entries per coarse index)
+  int rext[3];       // entries used per coarse index, per axis
 };
 
 struct Dev {
@@ -93,6 +95,7 @@ struct Dev {
   unsigned int* count;  // last-block counters, one per reduction site
   // solid table
   const signed char* solid_tab;
+  const signed char* clear_tab;  // 1 when no solid cell lies in the 3x3 (x, y) window
   int tab_w, tab_h;
 
   // multigrid
@@ -112,6 +115,12 @@ struct Dev {
   void* c0;                  // 6 N level-0 face coefficients for the V-cycle (float or bf16)
   unsigned int* hstate;      // hierarchy audit state
   const int* stencil_tab;    // 3 ints per offset, all levels
+  const int* stencil_lin;    // linear offset per stencil entry (interior cells)
+  const int* rt_idx;         // restriction tables: fine coordinate (-1 outside)
+  const float* rt_w;         // restriction tables: axis weight
+  unsigned char* mgnb0;      // level-0 neighbour-active bits
+  int* mgcol;                // ELL columns of levels >= 1, same layout as mgell
+  int mg_bottom;             // first level solved by the single-block bottom kernel
 };
 
 // Reduction sites (one last-block counter each).

@@ -212,6 +212,12 @@ struct Geo {
   }
 };
 
+// Source faces of the extension are stored as packed lattice coordinates z<<22 | y<<11 | x; within
+// one component lattice this orders exactly like the face index (the tie-break of
+// coupled_motion.glslinc:441).
+DI int pack_face(I3 q) { return (q.z << 22) | (q.y << 11) | q.x; }
+DI I3 unpack_coords(int p) { return mk(p & 2047, (p >> 11) & 2047, p >> 22); }
+
 DI bool geometry_on(const Dev& D) { return !(D.c[4] > .5 && D.c[5] < .5); }
 DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
 DI bool post_on(const Dev& D) { return D.c[4] > .5 && D.c[6] > .5 && D.c[7] < .5; }
@@ -334,7 +340,7 @@ __global__ void __launch_bounds__(NT) k_ext_init(Dev D) {
   int axis;
   g.unpack_face(f, q, axis);
   I3 l = ax(q, axis, -1);
-  D.src0[f] = (!g.wall_face(q, axis) && (g.wet(q) || g.wet(l))) ? (int)f : -1;
+  D.src0[f] = (!g.wall_face(q, axis) && (g.wet(q) || g.wet(l))) ? pack_face(q) : -1;
 }
 __global__ void __launch_bounds__(NT) k_ext_step(Dev D, int rb) {
   if (!post_on(D)) return;
@@ -350,10 +356,7 @@ __global__ void __launch_bounds__(NT) k_ext_step(Dev D, int rb) {
   float best = 1e20f;
   if (!g.wall_face(q, axis)) {
     if (source >= 0) {
-      I3 sq;
-      int sa;
-      g.unpack_face(source, sq, sa);
-      F3 dl = g.periodic_delta(q, sq);
+      F3 dl = g.periodic_delta(q, unpack_coords(source));
       best = dot3(dl, dl);
     }
     for (int a = 0; a < 3; a++)
@@ -362,10 +365,7 @@ __global__ void __launch_bounds__(NT) k_ext_step(Dev D, int rb) {
         if (!g.face_in_bounds(nb, axis) || g.wall_face(nb, axis)) continue;
         int cs = in[g.face_local(nb, axis)];
         if (cs < 0) continue;
-        I3 sq;
-        int sa;
-        g.unpack_face(cs, sq, sa);
-        F3 delta = g.periodic_delta(q, sq);
+        F3 delta = g.periodic_delta(q, unpack_coords(cs));
         float distance = dot3(delta, delta);
         if (distance < best || (distance == best && cs < source)) {
           best = distance;
@@ -383,12 +383,10 @@ DI bool projected_face(const Grid& g, I3 q, int axis) {
   if (!g.face_in_bounds(q, axis) || g.wall_face(q, axis)) return false;
   return g.wet(q) || g.wet(ax(q, axis, -1));
 }
-DI float extended_value(const Dev& D, const Grid& g, const float* Cb, long long source, I3 target) {
-  float value = Cb[D.N + source];
+DI float extended_value(const Dev& D, const Grid& g, const float* Cb, int packed, int component, I3 target) {
+  I3 q = unpack_coords(packed);
+  float value = Cb[D.N + g.face_local_raw(q, component)];
   if (!D.linear_air) return value;
-  I3 q;
-  int component;
-  g.unpack_face(source, q, component);
   F3 gradient = mf(0.f, 0.f, 0.f);
   for (int axis = 0; axis < 3; axis++) {
     I3 l = g.wrap_face(ax(q, axis, -1)), r = g.wrap_face(ax(q, axis, 1));
@@ -424,13 +422,13 @@ __global__ void __launch_bounds__(NT) k_ext_write(Dev D) {
     float value;
     if (air) {
       int source = D.src1[canonical];
-      value = source < 0 ? 0.f : extended_value(D, g, Cb, source, cq);
+      value = source < 0 ? 0.f : extended_value(D, g, Cb, source, axis, cq);
     } else
       value = Cb[D.N + canonical];
     Cb[D.N + f] = value;
   } else if (air) {
     int source = D.src1[f];
-    Cb[D.N + f] = source < 0 ? 0.f : extended_value(D, g, Cb, source, q);
+    Cb[D.N + f] = source < 0 ? 0.f : extended_value(D, g, Cb, source, axis, q);
   }
 }
 

@@ -24,7 +24,7 @@ DI bool phase_on(const Dev& D, int phase) {
   return c[4] > .5 && c[6] < .5;
 }
 
-DI int pmod(int x, int m) { return x >= 0 ? x % m : (m - 1) - ((-1 - x) % m); }
+DI int pmod(int x, int m) { return pidx(x, m); }
 
 struct MG {
   const Dev& D;
@@ -149,10 +149,18 @@ struct MG {
     }
     const MGLevelDev& lv = D.lv[l];
     const T* ell = (const T*)D.mgell + lv.eoff;
-    for (int k = 0; k < lv.stencil; k++) {
-      int j = wrap(l, addI(q, offset(l, k)));
-      sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[j > 0 ? j : 0]);
+    if (q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2) {
+      // every stencil point is inside: the neighbour is i + linear offset, no wrap
+      const int* lin = D.stencil_lin + lv.soff;
+#pragma unroll 8
+      for (int k = 0; k < lv.stencil; k++) sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[i + __ldg(lin + k)]);
+      return sum;
     }
+    // cached columns max(j, 0) (pressure_multigrid.glslinc:180), static geometry
+    const int* col = D.mgcol + lv.eoff;
+#pragma unroll 8
+    for (int k = 0; k < lv.stencil; k++)
+      sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[__ldg(col + (long long)k * lv.count + i)]);
     return sum;
   }
 };
@@ -479,112 +487,71 @@ template <class T> __global__ void k_mg_chol(Dev D, int l) {
 }
 
 // ---------------------------------------------------------------- V-cycle
-template <class T> __global__ void __launch_bounds__(NT) k_mg_load(Dev D, int phase) {
-  if (!phase_on(D, phase)) return;
-  long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  if (i >= D.N) return;
-  T* v = (T*)D.mgv;
-  long long M = D.mg_nodes;
-  v[i] = st_val<T>(D.r[i]);
-  v[M + i] = st_val<T>(0.f);
-  v[2 * M + i] = st_val<T>(0.f);
-}
-// 4th-kind Chebyshev sweep k (pressure_multigrid.glslinc:192-196)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_cheb(Dev D, int phase, int l, int source, int k) {
-  if (!phase_on(D, phase)) return;
-  MG m(D);
-  int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+// Per-cell operations, shared by the grid kernels and by the single-block bottom solver.
+template <class T> DI void cheb_cell(const MG& m, int l, int source, int k, int i, bool src_zero) {
   float c1 = (float)(2 * k - 3) / (float)(2 * k + 1), c2 = (float)(8 * k - 4) / (float)(2 * k + 1);
-  float r = ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, source, i);
+  const T* x = m.field<T>(source, l);
+  // A zero iterate makes apply() exactly +0, so r = b exactly; skip the operator.
+  float r = src_zero ? ld_val(m.field<T>(0, l)[i]) : ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, source, i);
   T* v7 = m.field<T>(7, l);
   float d = (k == 1 ? 0.f : c1 * ld_val(v7[i])) + c2 * ld_val(m.field<T>(4, l)[i]) * r;
-  float x = ld_val(m.field<T>(source, l)[i]) + d;
+  float xv = (src_zero ? 0.f : ld_val(x[i])) + d;
   v7[i] = st_val<T>(d);
-  m.field<T>(3 - source, l)[i] = st_val<T>(x);
+  m.field<T>(3 - source, l)[i] = st_val<T>(xv);
 }
-// Jacobi sweeps: op 14 (first, from zero) and op 6
-template <class T> __global__ void __launch_bounds__(NT) k_mg_jacobi(Dev D, int phase, int l, int source, int first) {
-  if (!phase_on(D, phase)) return;
-  MG m(D);
-  int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+template <class T> DI void jacobi_cell(const MG& m, int l, int source, int first, int i) {
   float s = ld_val(m.field<T>(4, l)[i]), b = ld_val(m.field<T>(0, l)[i]);
   if (first) m.field<T>(2, l)[i] = st_val<T>(s * b);
   else m.field<T>(3 - source, l)[i] = st_val<T>(ld_val(m.field<T>(source, l)[i]) + s * (b - m.apply<T>(l, source, i)));
 }
-// op 7: residual
-template <class T> __global__ void __launch_bounds__(NT) k_mg_residual(Dev D, int phase, int l, int f) {
-  if (!phase_on(D, phase)) return;
-  MG m(D);
-  int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+template <class T> DI void residual_cell(const MG& m, int l, int f, int i) {
   m.field<T>(6, l)[i] = st_val<T>(ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, f, i));
 }
-// op 8: exact P^T restriction into level l (pressure_multigrid.glslinc:200-224)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_restrict(Dev D, int phase, int l) {
-  if (!phase_on(D, phase)) return;
-  MG m(D);
-  int i = blockIdx.x * NT + threadIdx.x;
+// op 8: exact P^T restriction into coarse level l (pressure_multigrid.glslinc:200-224); the
+// per-axis weights come from the tables built with the same arithmetic at set-up.
+template <class T> DI void restrict_cell(const MG& m, int l, int i) {
+  const Dev& D = m.D;
   const MGLevelDev& cv = D.lv[l];
-  if (i >= cv.count) return;
   const int parent = l - 1;
   const MGLevelDev& pv = D.lv[parent];
-  int f[3] = {pv.fx, pv.fy, pv.fz}, nf[3] = {pv.nx, pv.ny, pv.nz}, nc[3] = {cv.nx, cv.ny, cv.nz};
   const T* r6 = m.field<T>(6, parent);
   float sum = 0.f;
   I3 qc = m.coord(l, i);
   if (m.active<T>(l, i)) {
     if (pv.aggregate) {
-      for (int z = 0; z < f[2]; z++)
-        for (int y = 0; y < f[1]; y++)
-          for (int x = 0; x < f[0]; x++) {
-            int j = m.wrap(parent, mk(qc.x * f[0] + x, qc.y * f[1] + y, qc.z * f[2] + z));
+      for (int z = 0; z < pv.fz; z++)
+        for (int y = 0; y < pv.fy; y++)
+          for (int x = 0; x < pv.fx; x++) {
+            int j = m.wrap(parent, mk(qc.x * pv.fx + x, qc.y * pv.fy + y, qc.z * pv.fz + z));
             if (m.active<T>(parent, j)) sum += ld_val(r6[j]);
           }
     } else {
-      int lo[3] = {qc.x * f[0], qc.y * f[1], qc.z * f[2]}, ext[3] = {1, 1, 1};
-      for (int a = 0; a < 3; a++)
-        if (f[a] > 1) {
-          lo[a]--;
-          ext[a] = 4;
-          if ((a == 2 || (a == 0 && D.px)) && nf[a] <= 4) { lo[a] = 0; ext[a] = nf[a]; }
-        }
-      for (int z = 0; z < ext[2]; z++)
-        for (int y = 0; y < ext[1]; y++)
-          for (int x = 0; x < ext[0]; x++) {
-            int j = m.wrap(parent, mk(lo[0] + x, lo[1] + y, lo[2] + z));
+      const int* ix = D.rt_idx + cv.roff[0] + 4 * qc.x;
+      const int* iy = D.rt_idx + cv.roff[1] + 4 * qc.y;
+      const int* iz = D.rt_idx + cv.roff[2] + 4 * qc.z;
+      const float* wx = D.rt_w + cv.roff[0] + 4 * qc.x;
+      const float* wy = D.rt_w + cv.roff[1] + 4 * qc.y;
+      const float* wz = D.rt_w + cv.roff[2] + 4 * qc.z;
+      for (int tz = 0; tz < cv.rext[2]; tz++)
+        for (int ty = 0; ty < cv.rext[1]; ty++) {
+          int fy = iy[ty];
+          if (fy < 0) continue;
+          for (int tx = 0; tx < cv.rext[0]; tx++) {
+            int fx = ix[tx];
+            if (fx < 0) continue;
+            int j = fx + pv.nx * (fy + pv.ny * iz[tz]);
             if (!m.active<T>(parent, j)) continue;
-            I3 q = m.coord(parent, j);
-            float weight = 1.f;
-            for (int a = 0; a < 3; a++) {
-              float pos = ((float)q[a] + .5f) / (float)f[a] - .5f;
-              int base = (int)floorf(pos);
-              float t = fract_(pos);
-              float w = 0.f;
-              for (int bit = 0; bit < f[a]; bit++) {
-                int nb = base + bit;
-                if (a == 2 || (a == 0 && D.px)) nb = pmod(nb, nc[a]);
-                else if (a == 0) nb = min(max(nb, 0), nc[a] - 1);
-                else nb = max(nb, 0);
-                if (nb == qc[a]) w += f[a] == 1 ? 1.f : (bit == 1 ? t : 1.f - t);
-              }
-              weight *= w;
-            }
+            float weight = 1.f * wx[tx] * wy[ty] * wz[tz];
             sum += weight * ld_val(r6[j]);
           }
+        }
     }
   }
   m.field<T>(0, l)[i] = st_val<T>(sum);
   m.field<T>(1, l)[i] = st_val<T>(0.f);
   m.field<T>(2, l)[i] = st_val<T>(0.f);
 }
-// op 9: prolongation-add
-template <class T> __global__ void __launch_bounds__(NT) k_mg_prolong(Dev D, int phase, int l, int ff, int cf) {
-  if (!phase_on(D, phase)) return;
-  MG m(D);
-  int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+template <class T> DI void prolong_cell(const MG& m, int l, int ff, int cf, int i) {
   float add = 0.f;
   if (m.active<T>(l, i)) {
     int ids[8];
@@ -596,11 +563,9 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_prolong(Dev D, int
   T* x = m.field<T>(ff, l);
   x[i] = st_val<T>(ld_val(x[i]) + add);
 }
-// op 12: coarse solve x = L^-T (L^-1 b), one block
-template <class T> __global__ void k_mg_coarse(Dev D, int phase, int l) {
-  if (!phase_on(D, phase)) return;
-  __shared__ float small[64];
-  MG m(D);
+// op 12: x = L^-T (L^-1 b), threads 0..n-1 of one block
+template <class T> DI void coarse_block(const MG& m, int l, float* small) {
+  const Dev& D = m.D;
   const int n = D.lv[l].count, t = threadIdx.x;
   const T* b = m.field<T>(0, l);
   if (t < n) {
@@ -614,8 +579,172 @@ template <class T> __global__ void k_mg_coarse(Dev D, int phase, int l) {
     for (int j = t; j < n; j++) d += D.mglinv[j * n + t] * small[j];
     m.field<T>(1, l)[t] = st_val<T>(d);
   }
+  __syncthreads();
 }
-// op 10 of the cycle + op 4 / op 9 finalisation
+
+// Level 0: 3-D thread mapping (x threads, y and z blocks), the neighbour-active bits of mgnb0.
+struct Cell0 {
+  int x, y, z;
+  long long i;
+  bool ok;
+};
+DI Cell0 cell0(const Dev& D) {
+  Cell0 c;
+  c.x = blockIdx.x * blockDim.x + threadIdx.x;
+  c.y = blockIdx.y;
+  c.z = blockIdx.z;
+  c.ok = c.x < D.nx;
+  c.i = (long long)(c.ok ? c.x : 0) + (long long)D.nx * ((long long)c.y + (long long)D.ny * c.z);
+  return c;
+}
+// apply at level 0 (pressure_multigrid.glslinc:93-99) with neighbour activity from one byte.
+template <class T> DI float apply0(const Dev& D, const T* x, const Cell0& c) {
+  unsigned m = D.mgnb0[c.i];
+  if (!(m & 64u)) return ld_val(x[c.i]);
+  const T* c0 = (const T*)D.c0;
+  const long long plane = (long long)D.nx * D.ny, N = D.N;
+  long long nb[6];
+  nb[0] = c.x > 0 ? c.i - 1 : c.i + (D.nx - 1);
+  nb[1] = c.x < D.nx - 1 ? c.i + 1 : c.i - (D.nx - 1);
+  nb[2] = c.i - D.nx;
+  nb[3] = c.i + D.nx;
+  nb[4] = c.z > 0 ? c.i - plane : c.i + plane * (D.nz - 1);
+  nb[5] = c.z < D.nz - 1 ? c.i + plane : c.i - plane * (D.nz - 1);
+  float here = ld_val(x[c.i]);
+  float sum = 0.f;
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    float other = (m >> f) & 1u ? ld_val(x[nb[f]]) : 0.f;
+    sum += ld_val(c0[(long long)f * N + c.i]) * (here - other);
+  }
+  return sum;
+}
+// Chebyshev sweep k at level 0; with fin >= 0 it is the last post-smoothing sweep and also does
+// op 10 of the cycle (z, partial sums) and the op 4 (phase 0) / op 9 (phase 1) finalisation.
+template <class T> __global__ void __launch_bounds__(NT) k_mg0_cheb(Dev D, int phase, int source, int k, int src_zero, int fin) {
+  if (!phase_on(D, phase)) return;
+  Cell0 c = cell0(D);
+  MG m(D);
+  float c1 = (float)(2 * k - 3) / (float)(2 * k + 1), c2 = (float)(8 * k - 4) / (float)(2 * k + 1);
+  double v[4] = {0, 0, 0, 0};
+  if (c.ok) {
+    const T* x = m.field<T>(source, 0);
+    float b = ld_val(m.field<T>(0, 0)[c.i]);
+    float r = src_zero ? b : b - apply0<T>(D, x, c);
+    T* v7 = m.field<T>(7, 0);
+    float d = (k == 1 ? 0.f : c1 * ld_val(v7[c.i])) + c2 * ld_val(m.field<T>(4, 0)[c.i]) * r;
+    float xv = (src_zero ? 0.f : ld_val(x[c.i])) + d;
+    T xs = st_val<T>(xv);
+    if (fin < 0) {
+      v7[c.i] = st_val<T>(d);
+      m.field<T>(3 - source, 0)[c.i] = xs;
+    } else {
+      float rr = D.r[c.i], z = ld_val(xs), bb = D.b[c.i];
+      D.z[c.i] = z;
+      if (phase == 0) D.d[c.i] = z;
+      v[0] = (double)rr * (double)z;
+      v[1] = (double)rr * (double)rr;
+      v[2] = (double)bb * (double)bb;
+      v[3] = (double)fabsf(rr);
+    }
+  }
+  if (fin < 0) return;
+  const int ops[4] = {0, 0, 0, 1};
+  double out[4];
+  if (last_block_reduce<NT, 4>(D, kSiteRZ, v, ops, out) && threadIdx.x == 0) {
+    if (phase == 0) finalize_op4(D, out);
+    else finalize_op9(D, out);
+  }
+}
+template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(Dev D, int phase, int f) {
+  if (!phase_on(D, phase)) return;
+  Cell0 c = cell0(D);
+  if (!c.ok) return;
+  MG m(D);
+  m.field<T>(6, 0)[c.i] = st_val<T>(ld_val(m.field<T>(0, 0)[c.i]) - apply0<T>(D, m.field<T>(f, 0), c));
+}
+// phase 0 load (op 5 of the cycle) fused with the first Chebyshev sweep from zero
+template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(Dev D, int phase, int first_sweep) {
+  if (!phase_on(D, phase)) return;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  T* v = (T*)D.mgv;
+  long long M = D.mg_nodes;
+  T b = st_val<T>(D.r[i]);
+  v[i] = b;
+  v[M + i] = st_val<T>(0.f);
+  v[2 * M + i] = st_val<T>(0.f);
+  if (first_sweep) {  // k = 1 from x = 0: r = b, d = 0 + c2 s b, x2 = 0 + d
+    float c2 = 4.f / 3.f;
+    float d = 0.f + c2 * ld_val(v[4 * M + i]) * ld_val(b);
+    v[7 * M + i] = st_val<T>(d);
+    v[2 * M + i] = st_val<T>(0.f + d);
+  }
+}
+
+// Generic levels (l >= 1): one thread per cell.
+template <class T> __global__ void __launch_bounds__(NT) k_mgl(Dev D, int phase, int op, int l, int a, int b, int c) {
+  if (!phase_on(D, phase)) return;
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  MG m(D);
+  switch (op) {
+    case 0: cheb_cell<T>(m, l, a, b, i, c != 0); break;
+    case 1: jacobi_cell<T>(m, l, a, b, i); break;
+    case 2: residual_cell<T>(m, l, a, i); break;
+    case 3: restrict_cell<T>(m, l, i); break;
+    case 4: prolong_cell<T>(m, l, a, b, i); break;
+  }
+}
+
+// Whole sub-cycle from level lb down to the coarsest and back, in one block.
+// Returns (in *out_field) the field holding the level-lb correction.
+template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(Dev D, int phase, int lb) {
+  if (!phase_on(D, phase)) return;
+  __shared__ float small[64];
+  MG m(D);
+  const int L = D.L;
+  int field[kMaxLevels];
+  auto each = [&](int l, auto fn) {
+    for (int i = threadIdx.x; i < D.lv[l].count; i += blockDim.x) fn(i);
+    __syncthreads();
+  };
+  auto smooth = [&](int l, int f, bool zero) {
+    for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
+      if (D.mg_smoother == 1) each(l, [&](int i) { cheb_cell<T>(m, l, f, sweep + 1, i, zero && sweep == 0); });
+      else each(l, [&](int i) { jacobi_cell<T>(m, l, f, zero && sweep == 0 ? 1 : 0, i); });
+      f = 3 - f;
+    }
+    return f;
+  };
+  for (int l = lb; l < L - 1; l++) {
+    int f = smooth(l, 1, true);
+    field[l] = f;
+    each(l, [&](int i) { residual_cell<T>(m, l, f, i); });
+    each(l + 1, [&](int i) { restrict_cell<T>(m, l + 1, i); });
+  }
+  int cf;
+  const int lc = L - 1;
+  if (D.lv[lc].count <= 64) {
+    coarse_block<T>(m, lc, small);
+    cf = 1;
+  } else {
+    cf = 1;
+    for (int sweep = 0; sweep < 32; sweep++) {
+      int f = cf;
+      each(lc, [&](int i) { jacobi_cell<T>(m, lc, f, sweep == 0 ? 1 : 0, i); });
+      cf = 3 - cf;
+    }
+  }
+  for (int l = L - 2; l >= lb; l--) {
+    int f = field[l];
+    int ccf = cf;
+    each(l, [&](int i) { prolong_cell<T>(m, l, f, ccf, i); });
+    cf = smooth(l, f, false);
+  }
+}
+
+// op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(Dev D, int phase, int f) {
   if (!phase_on(D, phase)) return;
   MG m(D);
@@ -644,42 +773,82 @@ template <class T> struct Cycle {
   const Dev& D;
   cudaStream_t s;
   int phase;
-  int smooth(int l, int field, bool zero) {
+  int fused_first;  // the level-0 first pre-smoothing sweep was done by the caller
+  dim3 grid0() const { return dim3((unsigned)((D.nx + NT - 1) / NT), (unsigned)D.ny, (unsigned)D.nz); }
+  int smooth(int l, int field, bool zero, bool last0) {
     unsigned gr = grid_for(D.lv[l].count);
     for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
-      if (D.mg_smoother == 1) k_mg_cheb<T><<<gr, NT, 0, s>>>(D, phase, l, field, sweep + 1);
-      else k_mg_jacobi<T><<<gr, NT, 0, s>>>(D, phase, l, field, zero && sweep == 0 ? 1 : 0);
+      bool first = zero && sweep == 0;
+      bool fin = last0 && sweep == D.mg_smoothing - 1;
+      if (l == 0 && first && fused_first) {
+        field = 3 - field;
+        continue;
+      }
+      if (D.mg_smoother == 1) {
+        if (l == 0) k_mg0_cheb<T><<<grid0(), NT, 0, s>>>(D, phase, field, sweep + 1, first ? 1 : 0, fin ? 1 : -1);
+        else k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 0, l, field, sweep + 1, first ? 1 : 0);
+      } else
+        k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 1, l, field, first ? 1 : 0, 0);
       field = 3 - field;
     }
     return field;
   }
+  // pre- and post-smoothing flip the field mg_smoothing times each: a level ends in field 1
+  int bottom_field() const { return 1; }
   int level(int l) {
     unsigned gr = grid_for(D.lv[l].count);
-    if (l == D.L - 1) {
-      if (D.lv[l].count <= 64) {
-        k_mg_coarse<T><<<1, 64, 0, s>>>(D, phase, l);
-        return 1;
+    if (l == D.L - 1 || l == D.mg_bottom) {
+      k_mg_bottom<T><<<1, 1024, 0, s>>>(D, phase, l);
+      if (l == D.L - 1) {
+        if (D.lv[l].count <= 64) return 1;
+        return 1;  // 32 Jacobi sweeps end in field 1
       }
-      int tf = 1;
-      for (int sweep = 0; sweep < 32; sweep++) {
-        k_mg_jacobi<T><<<gr, NT, 0, s>>>(D, phase, l, tf, sweep == 0 ? 1 : 0);
-        tf = 3 - tf;
-      }
-      return tf;
+      return bottom_field();
     }
-    int field = smooth(l, 1, true);
-    k_mg_residual<T><<<gr, NT, 0, s>>>(D, phase, l, field);
-    k_mg_restrict<T><<<grid_for(D.lv[l + 1].count), NT, 0, s>>>(D, phase, l + 1);
+    int field = smooth(l, 1, true, false);
+    if (l == 0) k_mg0_residual<T><<<grid0(), NT, 0, s>>>(D, phase, field);
+    else k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 2, l, field, 0, 0);
+    k_mgl<T><<<grid_for(D.lv[l + 1].count), NT, 0, s>>>(D, phase, 3, l + 1, 0, 0, 0);
     int cf = level(l + 1);
-    k_mg_prolong<T><<<gr, NT, 0, s>>>(D, phase, l, field, cf);
-    return smooth(l, field, false);
+    k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 4, l, field, cf, 0);
+    return smooth(l, field, false, l == 0 && D.mg_smoother == 1);
   }
   void run() {
-    if (phase == 0) k_mg_load<T><<<grid_for(D.N), NT, 0, s>>>(D, phase);
+    if (phase == 0) k_mg0_load<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, D.mg_smoother == 1 ? 1 : 0);
+    fused_first = D.mg_smoother == 1;
     int f = level(0);
-    k_mg_finish<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, f);
+    // Chebyshev smoothing fuses z and the finalisation into the last level-0 sweep
+    if (D.mg_smoother != 1) k_mg_finish<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, f);
   }
 };
+
+// Columns of the ELL rows, max(wrap(l, q + offset), 0), computed once (static geometry).
+__global__ void __launch_bounds__(NT) k_mg_cols(Dev D, int l) {
+  MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  int i = blockIdx.x * NT + threadIdx.x;
+  if (i >= lv.count) return;
+  I3 q = m.coord(l, i);
+  for (int k = 0; k < lv.stencil; k++) {
+    int j = m.wrap(l, addI(q, m.offset(l, k)));
+    D.mgcol[lv.eoff + (long long)k * lv.count + i] = j > 0 ? j : 0;
+  }
+}
+
+// Level-0 neighbour-active bits (bit f: neighbour across face f active, bit 6: cell active),
+// rebuilt after the masks on structural rebuilds.
+template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(Dev D) {
+  if (!build_on(D) || D.hstate[9] == 0) return;
+  MG m(D);
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  I3 q = m.coord(0, (int)i);
+  unsigned bits = m.active<T>(0, (int)i) ? 64u : 0u;
+  for (int axis = 0; axis < 3; axis++)
+    for (int side = 0; side < 2; side++)
+      if (m.active<T>(0, m.wrap(0, ax(q, axis, 2 * side - 1)))) bits |= 1u << (2 * axis + side);
+  D.mgnb0[i] = (unsigned char)bits;
+}
 
 template <class T> void build(const Dev& D, cudaStream_t s) {
   k_hs_reset<<<1, 1, 0, s>>>(D);
@@ -687,6 +856,7 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
   k_hs_decide<<<1, 1, 0, s>>>(D);
   k_hs_snapshot<T><<<grid_for(D.N), NT, 0, s>>>(D);
   for (int l = 0; l < D.L; l++) k_mg_mask<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  k_mg_nb0<T><<<grid_for(D.N), NT, 0, s>>>(D);
   for (int l = 0; l + 1 < D.L; l++) k_mg_transfer<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
   k_mg_scale<T><<<grid_for(D.lv[0].count), NT, 0, s>>>(D, 0);
   for (int l = 1; l < D.L; l++) {
@@ -712,6 +882,9 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
 
 }  // namespace
 
+void launch_mg_cols(const Dev& D, cudaStream_t s) {
+  for (int l = 1; l < D.L; l++) k_mg_cols<<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+}
 void mg_kernel_attributes() {
   cudaFuncSetAttribute(k_mg_galerkin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
   cudaFuncSetAttribute(k_mg_galerkin<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
@@ -721,8 +894,8 @@ void launch_mg_build(const Dev& D, cudaStream_t s) {
   else build<float>(D, s);
 }
 void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase) {
-  if (D.bf16) Cycle<__nv_bfloat16>{D, s, phase}.run();
-  else Cycle<float>{D, s, phase}.run();
+  if (D.bf16) Cycle<__nv_bfloat16>{D, s, phase, 0}.run();
+  else Cycle<float>{D, s, phase, 0}.run();
 }
 
 }  // namespace wg

@@ -301,8 +301,49 @@ struct Mac {
     valid = vb[f] > .5f;
     return parity * (forward ? D.fwd[f] : m.A[D.N + f]);
   }
-  // sampled_component (coupled_motion.glslinc:112-137)
-  __device__ __noinline__ float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
+  // sampled_component (coupled_motion.glslinc:112-137).  Fast path: when the donor block's corner
+  // lo is inside the domain and no solid cell lies in the 3x3 (x, y) window around it, every
+  // donor is a plain stored face (no reflection, ghost or wall branch applies, parity 1), so the
+  // donor lookups reduce to two loads each; the arithmetic is unchanged.
+  DI float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
+    const Dev& D = m.D;
+    F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);
+    lattice[axis] += .5f;
+    I3 lo = mk((int)floorf(lattice.x), (int)floorf(lattice.y), (int)floorf(lattice.z));
+    if ((D.flags & 8) == 0 && !D.px && lo.x >= 0 && lo.y >= 0 && lo.x + 1 < D.nx + (axis == 0) &&
+        lo.y + 1 < D.ny + (axis == 1) && lo.x + kSolidPad < D.tab_w && lo.y + kSolidPad < D.tab_h &&
+        D.clear_tab[(lo.y + kSolidPad) * D.tab_w + lo.x + kSolidPad]) {
+      F3 t = mf(fract_(lattice.x), fract_(lattice.y), fract_(lattice.z));
+      lim0 = 1e20f;
+      lim1 = -1e20f;
+      valid = true;
+      const int mx_ = D.nx + (axis == 0), my_ = D.ny + (axis == 1);
+      const long long base = axis == 0 ? 0 : (axis == 1 ? D.NU : D.NU + D.NV);
+      const float* src = forward ? D.fwd : m.A + D.N;
+      float values[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        int xx = c & 1, y = (c >> 1) & 1, z = c >> 2;
+        int qz = pidx(lo.z + z, D.nz);  // wrap; a face at z = nz is the canonical z = 0
+        long long f = base + (long long)(lo.x + xx) + (long long)mx_ * ((long long)(lo.y + y) + (long long)my_ * qz);
+        bool supported = vb[f] > .5f;
+        float value = src[f];
+        values[c] = value;
+        float wx = xx ? t.x : 1.f - t.x, wy = y ? t.y : 1.f - t.y, wz = z ? t.z : 1.f - t.z;
+        if (wx * wy * wz > 0.f) {
+          valid = valid && supported;
+          lim0 = mnf(lim0, value);
+          lim1 = mxf(lim1, value);
+        }
+      }
+      float a = __fmaf_rn(t.x, values[1] - values[0], values[0]), b = __fmaf_rn(t.x, values[3] - values[2], values[2]);
+      float d = __fmaf_rn(t.x, values[5] - values[4], values[4]), e = __fmaf_rn(t.x, values[7] - values[6], values[6]);
+      float lower = __fmaf_rn(t.y, b - a, a), upper = __fmaf_rn(t.y, e - d, d);
+      return __fmaf_rn(t.z, upper - lower, lower);
+    }
+    return sample_slow(x, axis, forward, valid, lim0, lim1);
+  }
+  __device__ __noinline__ float sample_slow(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
     const Grid& g = m.g;
     const Dev& D = m.D;
     F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);

@@ -107,9 +107,16 @@ template <class T> __global__ void __launch_bounds__(NT) k_cg_update(Dev D) {
   D.r[i] = r;
   T* v = (T*)D.mgv;
   long long M = D.mg_nodes;
-  v[i] = st_val<T>(r);      // field 0 rhs
-  v[M + i] = st_val<T>(0.f);  // field 1
-  v[2 * M + i] = st_val<T>(0.f);  // field 2
+  T b = st_val<T>(r);
+  v[i] = b;                      // field 0 rhs (op 5 of the cycle)
+  v[M + i] = st_val<T>(0.f);     // field 1
+  if (D.mg_smoother == 1) {
+    // first level-0 Chebyshev sweep (k = 1) from x = 0: r = b, d = 0 + c2 s b, x2 = 0 + d
+    float d = 0.f + (4.f / 3.f) * ld_val(v[4 * M + i]) * ld_val(b);
+    v[7 * M + i] = st_val<T>(d);
+    v[2 * M + i] = st_val<T>(0.f + d);
+  } else
+    v[2 * M + i] = st_val<T>(0.f);
 }
 
 // ---------------------------------------------------------------- op 10 (+ loop condition)

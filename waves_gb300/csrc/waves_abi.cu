@@ -299,6 +299,18 @@ waves_status setup_device(waves_handle* h) {
     AL(dtab, tab.size(), false, "solid_table");
     CK(cudaMemcpyAsync(dtab, tab.data(), tab.size(), cudaMemcpyHostToDevice, h->stream));
     D.solid_tab = dtab;
+    std::vector<signed char> clear(tab.size(), 0);
+    for (int y = 1; y + 1 < D.tab_h; y++)
+      for (int x = 1; x + 1 < D.tab_w; x++) {
+        bool any = false;
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) any = any || tab[(size_t)(y + dy) * D.tab_w + x + dx] != 0;
+        clear[(size_t)y * D.tab_w + x] = any ? 0 : 1;
+      }
+    signed char* dclear;
+    AL(dclear, clear.size(), false, "clear_table");
+    CK(cudaMemcpyAsync(dclear, clear.data(), clear.size(), cudaMemcpyHostToDevice, h->stream));
+    D.clear_tab = dclear;
     CK(cudaStreamSynchronize(h->stream));
   }
   // multigrid
@@ -346,6 +358,89 @@ waves_status setup_device(waves_handle* h) {
     AL(dst, h->stencil_tab.size(), false, "stencils");
     CK(cudaMemcpyAsync(dst, h->stencil_tab.data(), h->stencil_tab.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     D.stencil_tab = dst;
+    // linear offsets of the stencil entries, per level (valid for cells two cells from every edge)
+    std::vector<int> lin(h->stencil_tab.size() / 3);
+    for (int l = 0; l < D.L; l++)
+      for (int k = 0; k < D.lv[l].stencil; k++) {
+        const int* o = &h->stencil_tab[3 * (D.lv[l].soff + k)];
+        lin[D.lv[l].soff + k] = o[0] + D.lv[l].nx * (o[1] + D.lv[l].ny * o[2]);
+      }
+    int* dlin;
+    AL(dlin, lin.size(), false, "stencil_linear");
+    CK(cudaMemcpyAsync(dlin, lin.data(), lin.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    D.stencil_lin = dlin;
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  // Restriction tables (pressure_multigrid.glslinc:208-221): for coarse level l, axis a, coarse
+  // index X, up to four fine coordinates and the axis weight, with the same float arithmetic.
+  {
+    std::vector<int> ridx;
+    std::vector<float> rw;
+    auto pm = [](int x, int m) { return x >= 0 ? x % m : (m - 1) - ((-1 - x) % m); };
+    for (int l = 1; l < D.L; l++) {
+      wg::MGLevelDev& cv = D.lv[l];
+      const wg::MGLevelDev& pv = D.lv[l - 1];
+      int nc[3] = {cv.nx, cv.ny, cv.nz}, nf[3] = {pv.nx, pv.ny, pv.nz}, fa[3] = {pv.fx, pv.fy, pv.fz};
+      for (int a = 0; a < 3; a++) {
+        bool periodic = a == 2 || (a == 0 && D.px);
+        int f = fa[a];
+        int ext = f > 1 ? ((periodic && nf[a] <= 4) ? nf[a] : 4) : 1;
+        cv.roff[a] = (int)ridx.size();
+        cv.rext[a] = ext;
+        for (int X = 0; X < nc[a]; X++) {
+          int lo = f > 1 ? ((periodic && nf[a] <= 4) ? 0 : X * f - 1) : X * f;
+          for (int t = 0; t < 4; t++) {
+            int q = lo + t, idx = -1;
+            float w = 0.f;
+            if (t < ext) {
+              if (periodic) q = pm(q, nf[a]);
+              if (q >= 0 && q < nf[a]) {
+                idx = q;
+                volatile float pos = ((float)q + .5f) / (float)f;
+                pos = pos - .5f;
+                int base = (int)std::floor((float)pos);
+                float tt = (float)pos - std::floor((float)pos);
+                for (int bit = 0; bit < f; bit++) {
+                  int nb = base + bit;
+                  if (periodic) nb = pm(nb, nc[a]);
+                  else if (a == 0) nb = std::min(std::max(nb, 0), nc[a] - 1);
+                  else nb = std::max(nb, 0);
+                  if (nb == X) w += f == 1 ? 1.f : (bit == 1 ? tt : 1.f - tt);
+                }
+              }
+            }
+            ridx.push_back(idx);
+            rw.push_back(w);
+          }
+        }
+      }
+    }
+    if (ridx.empty()) {
+      ridx.push_back(-1);
+      rw.push_back(0.f);
+    }
+    int* di;
+    float* dw;
+    AL(di, ridx.size(), false, "restrict_idx");
+    AL(dw, rw.size(), false, "restrict_w");
+    CK(cudaMemcpyAsync(di, ridx.data(), ridx.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dw, rw.data(), rw.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    D.rt_idx = di;
+    D.rt_w = dw;
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  AL(D.mgnb0, N, true, "mg_level0_neighbours");
+  AL(D.mgcol, eoff, false, "mg_ell_columns");
+  // Levels from mg_bottom down run inside one thread block (latency-bound sizes).
+  D.mg_bottom = D.L - 1;
+  for (int l = 1; l < D.L; l++)
+    if (D.lv[l].count <= 1024) {
+      D.mg_bottom = l;
+      break;
+    }
+  if (const char* e = getenv("WAVES_MG_BOTTOM")) {
+    int v = atoi(e);
+    if (v >= 1 && v < D.L) D.mg_bottom = v;
   }
   AL(D.mgmat, moff, true, "mg_matrix");
   {
@@ -642,6 +737,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
     }
   }
   if ((st = setup_device(h)) != WAVES_OK) return fail(st);
+  wg::launch_mg_cols(h->D, h->stream);
   wg::launch_initial(h->D, h->stream, h->probes);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     h->err = "initial commands failed";
