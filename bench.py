@@ -154,6 +154,10 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     motion, pressure, trials = timing(True)
     c1 = s.control()
+    # Roofline of the dominant kernel: one further step, host-scheduled, with every launch of the
+    # probed kernels bracketed by CUDA events on the solver's stream (outside the timed region).
+    s.request_steps(int(c1[2]) + 1)
+    probe_trials, probes = s.probe_trial()
     sim = c1[1] - c0[1]
     dev_s = (motion + pressure) / 1e3
     counts = (C.c_int32 * 8)()
@@ -171,6 +175,7 @@ def run_ours(args, world, rank, local):
         "motion_ms": motion, "pressure_ms": pressure, "iters": iters, "defect_rounds": rounds - active,
         "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
         "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
+        "probes": probes if probe_trials else [],
     }
     # e2e: frames through the public API with host buffers
     e2e = None
@@ -191,6 +196,56 @@ def run_ours(args, world, rank, local):
     out["e2e"] = e2e
     s.close()
     return out
+
+
+def measured_peaks():
+    """HBM copy bandwidth (GB/s) measured on this GPU model, else the stated fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the probed kernels
+    from the ncu captures summarised in profiles/dram_traffic.txt ('kernel bytes ...' lines)."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and not line.startswith("#"):
+                    try:
+                        out[parts[0]] = float(parts[1])
+                    except ValueError:
+                        pass
+    except OSError:
+        pass
+    return out
+
+
+def roofline(probes):
+    """HBM roofline of the kernel with the largest probed time in one trial: algorithmic bytes per
+    launch / CUDA-event time per launch, against the measured copy bandwidth."""
+    live = [p for p in probes if p["launches"] > 0 and p["ms"] > 0]
+    if not live:
+        return None, []
+    peak, source = measured_peaks()
+    total = sum(p["ms"] for p in live)
+    table = []
+    for p in live:
+        gbs = p["bytes"] / (p["ms"] / 1e3) / 1e9
+        table.append({"kernel": p["kernel"], "launches": p["launches"], "us_per_launch": 1e3 * p["ms"] / p["launches"],
+                      "bytes_per_launch": p["bytes"] / p["launches"], "achieved_gbs": gbs, "frac": gbs / peak,
+                      "share_of_probed": p["ms"] / total})
+    top = max(table, key=lambda t: t["us_per_launch"] * t["launches"])
+    traffic = ncu_traffic().get(top["kernel"])
+    return {"bound": "hbm", "kernel": top["kernel"], "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
+            "frac": top["frac"], "peak_source": f"{source} copy bandwidth (hbm_gbs)",
+            "traffic": traffic, "bytes_per_launch": top["bytes_per_launch"], "us_per_launch": top["us_per_launch"],
+            "launches": top["launches"],
+            "timing": "CUDA events on the solver stream around each launch, one host-scheduled trial after the timed steps"}, table
 
 
 def cpu_baseline(args, cfg_mg, seconds):
@@ -251,7 +306,7 @@ def main():
     steps = max(res["steps"], 1)
     line = {
         "metric": METRIC,
-        "value": sim_total / dev_max,
+        "value": sim_total / dev_max if dev_max > 0 else None,
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
@@ -276,6 +331,9 @@ def main():
         "clocks": res["clocks"],
         "gpu_launches": res["launches"],
     }
+    roof, kernels = roofline(res["probes"])
+    line["roofline"] = roof
+    line["probed_kernels"] = kernels
     if res["e2e"]:
         e = res["e2e"]
         line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

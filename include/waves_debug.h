@@ -22,6 +22,19 @@ waves_status waves_debug_sample(waves_handle* h, const float* x, int32_t axis, i
  * projection/extension/acceptance, trial end, condition kernel. */
 waves_status waves_debug_launch_counts(waves_handle* h, int32_t* out8);
 waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size_t bytes);
+/* Kernel probes of one host-scheduled trial (every CG iteration checked, so no probed launch is a
+ * no-op): per kind, the launches, their summed CUDA-event time on the handle's stream and their
+ * summed algorithmic bytes (distinct inputs read once, outputs written once).  Kinds: 0 MacCormack
+ * passes, 1 level-0 Chebyshev sweeps, 2 level >= 1 sweeps (product-parallel rows), 3 level >= 1
+ * sweeps (one thread per row), 4 VOF flux + update.  The trial advances the simulation like any
+ * other; *trials is 0 when no trial was active (quota met). */
+typedef struct waves_kernel_probe {
+  int32_t kind;
+  int32_t launches;
+  double ms;
+  double bytes;
+} waves_kernel_probe;
+waves_status waves_debug_probe_trial(waves_handle* h, waves_kernel_probe* out, int32_t capacity, int32_t* trials);
 #ifdef __cplusplus
 }
 #endif

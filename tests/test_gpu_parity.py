@@ -68,3 +68,22 @@ def test_step_parity(gpu_lib, name):
         problems = compare_state(g, o, cfg, f"step {step}")
         assert not problems, "\n".join(problems)
     assert g.control()[2] == STEPS
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["beach_slope", "beach_slope_bf16"])
+def test_step_parity_row_per_thread(gpu_lib, name, monkeypatch):
+    """The multigrid levels >= 1 have two apply kernels (product-parallel rows for small levels,
+    one thread per row for large ones); the small grids above use only the first, so force the
+    second on every level here."""
+    monkeypatch.setenv("WAVES_MG_ROWS_BELOW", "0")
+    cfg = CASES[name]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for step in range(1, 4):
+        g.request_steps(step)
+        g.run()
+        o.request_steps(step)
+        o.run()
+        problems = compare_state(g, o, cfg, f"step {step}")
+        assert not problems, "\n".join(problems)

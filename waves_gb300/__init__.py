@@ -126,6 +126,16 @@ class WavesSolver:
         arr = np.ascontiguousarray(c, dtype=np.float64)
         self._ck(self.lib.waves_set_control(self.h, arr.ctypes.data_as(C.POINTER(C.c_double)), len(arr)))
 
+    def probe_trial(self):
+        """Run one host-scheduled trial with kernel probes (waves_debug_probe_trial): per probed
+        kernel, launches, summed CUDA-event milliseconds and summed algorithmic bytes."""
+        from .abi import PROBE_KINDS, WavesKernelProbe
+        out = (WavesKernelProbe * len(PROBE_KINDS))()
+        trials = C.c_int32()
+        self._ck(self.lib.waves_debug_probe_trial(self.h, out, len(PROBE_KINDS), C.byref(trials)))
+        return trials.value, [{"kernel": PROBE_KINDS[k], "launches": out[k].launches, "ms": out[k].ms,
+                               "bytes": out[k].bytes} for k in range(len(PROBE_KINDS))]
+
     def inject_rejection(self):
         self._ck(self.lib.waves_inject_rejection(self.h))
 

@@ -131,6 +131,19 @@ class WavesWarmStartModel(C.Structure):
     ]
 
 
+class WavesKernelProbe(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("launches", C.c_int32),
+        ("ms", C.c_double),
+        ("bytes", C.c_double),
+    ]
+
+
+# Kinds of waves_debug_probe_trial (include/waves_debug.h): the kernel each probes.
+PROBE_KINDS = ["k_mac", "k_mg0_cheb", "k_mgl_rows", "k_mgl", "k_sweep_update"]
+
+
 # Every function declared in include/waves.h.
 WAVES_ABI_SYMBOLS = [
     "waves_config_default",
@@ -206,6 +219,7 @@ def declare(lib):
     sig["waves_debug_sample"] = (C.c_int, [h, P(C.c_float), C.c_int32, C.c_int32, P(C.c_float)])
     sig["waves_debug_launch_counts"] = (C.c_int, [h, P(C.c_int32)])
     sig["waves_debug_read"] = (C.c_int, [h, C.c_char_p, C.c_void_p, C.c_size_t])
+    sig["waves_debug_probe_trial"] = (C.c_int, [h, P(WavesKernelProbe), C.c_int32, P(C.c_int32)])
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res

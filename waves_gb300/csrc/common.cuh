@@ -243,10 +243,45 @@ struct Coast {
     p[axis] -= .5f * g.h(axis);
     return p;
   }
+  // Tabulated forms (entries are these same functions of the same arguments, so a lookup and a
+  // direct evaluation give identical bits).
+  DI int slot_of(float time) const {
+    const float* s = D.wstamp;
+    if (!s) return -1;
+    return time == s[0] ? 0 : (time == s[1] ? 1 : (time == s[2] ? 2 : -1));
+  }
+  // surface() at the centre of cell column x
+  DI void surface_col(const Grid& g, int x, float time, float& s0, float& s1) const {
+    const int j = x - D.wt_x0;
+    int sl;
+    if (j >= 0 && j < D.wt_w && (sl = slot_of(time)) >= 0) {
+      const float2 v = D.wsurf[sl * D.wt_w + j];
+      s0 = v.x;
+      s1 = v.y;
+      return;
+    }
+    surface(g.center(mk(x, 0, 0)).x, time, s0, s1);
+  }
+  // velocity_c() at the position of face (q, axis); z does not enter the wave target
+  DI float velocity_face(const Grid& g, I3 q, int axis, float time) const {
+    if (axis == 2) return 0.f;
+    const int j = q.x - D.wt_x0;
+    int sl;
+    if (j >= 0 && j < D.wt_w && q.y >= 0 && q.y < D.wt_h && (sl = slot_of(time)) >= 0)
+      return D.wvel[((sl * 2 + axis) * D.wt_h + q.y) * D.wt_w + j];
+    return velocity_c(face_position(g, q, axis), time, axis);
+  }
+  // relaxation factor 1 - exp(-rate dt) at a cell centre (axis < 0) or a face position
+  DI float relax(const Grid& g, I3 q, int axis, float dt) const {
+    const int j = q.x - D.wt_x0;
+    if (D.wstamp && dt == D.wstamp[3] && j >= 0 && j < D.wt_w) return D.wdecay[(axis == 0 ? D.wt_w : 0) + j];
+    const F3 p = axis < 0 ? g.center(q) : face_position(g, q, axis);
+    return 1.f - texp(-rate(p.x) * dt);
+  }
   DI float4 plane(const Grid& g, I3 q, float time) const {
     float s0, s1;
     F3 cq = g.center(q);
-    surface(cq.x, time, s0, s1);
+    surface_col(g, q.x, time, s0, s1);
     F3 normal = mf(-s1 * D.hx, D.hy, 0.f);
     return make_float4(normal.x, normal.y, normal.z, half_dot(normal) + s0 - cq.y);
   }

@@ -60,6 +60,15 @@ struct Dev {
   double cell_d;  // hx*hy*hz in double
   // coastal zone: x columns [0, zone_x_end) hold every cell/face with a nonzero relaxation rate
   int zone_x_end;
+  // Wave-target tables, rebuilt every trial for the trial's three times (accepted, CFL look-ahead,
+  // new): surface per cell column, u and v target velocities per face column and row, and the
+  // relaxation factor per column for the trial's dt.  wstamp holds the three times and that dt;
+  // a lookup whose time (or dt) is not stamped, or whose column/row is outside, evaluates directly.
+  float2* wsurf;   // [3][wt_w]
+  float* wvel;     // [3][2][wt_h][wt_w]
+  float* wdecay;   // [2][wt_w]: cell centres, u faces
+  float* wstamp;   // [4]
+  int wt_x0, wt_w, wt_h;
 
   // physical banks [F | u | v | w | p]
   float* bank0;
@@ -96,6 +105,10 @@ struct Dev {
   // solid table
   const signed char* solid_tab;
   const signed char* clear_tab;  // 1 when no solid cell lies in the 3x3 (x, y) window
+  const unsigned char* mac_class;  // per (axis, y, x) face column: 1 near a solid cell or the domain edge
+  int* mac_list;                 // MacCormack work list (faces)
+  unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
+  int mac_grid;                  // persistent MacCormack blocks
   int tab_w, tab_h;
 
   // multigrid
@@ -121,6 +134,7 @@ struct Dev {
   unsigned char* mgnb0;      // level-0 neighbour-active bits
   int* mgcol;                // ELL columns of levels >= 1, same layout as mgell
   int mg_bottom;             // first level solved by the single-block bottom kernel
+  int mg_rows_below;         // levels with fewer rows use the product-parallel apply
 };
 
 // Reduction sites (one last-block counter each).

@@ -223,7 +223,7 @@ DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
 DI bool post_on(const Dev& D) { return D.c[4] > .5 && D.c[6] > .5 && D.c[7] < .5; }
 
 // ---------------------------------------------------------------- op 17 (+ coastal op 87/88)
-__global__ void __launch_bounds__(NT) k_geom_plane(Dev D, int op, int with_bounds) {
+__global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D, int op, int with_bounds) {
   bool on = op == 19 ? !(D.c[4] > .5) : geometry_on(D);
   bool bounds = with_bounds && setup_on(D);
   if (!on && !bounds) return;
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(NT) k_geom_plane(Dev D, int op, int with_bound
 }
 
 // ---------------------------------------------------------------- op 18
-__global__ void __launch_bounds__(NT) k_geom_phi(Dev D) {
+__global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) {
   if (!geometry_on(D)) return;
   Geo G(D, 18);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(NT) k_geom_phi(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 16
-__global__ void __launch_bounds__(NT) k_geom_coef(Dev D) {
+__global__ void __launch_bounds__(NT) k_geom_coef(const __grid_constant__ Dev D) {
   if (!geometry_on(D)) return;
   Geo G(D, 16);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(NT) k_geom_coef(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 2 + op 47
-__global__ void __launch_bounds__(NT) k_proj_setup(Dev D) {
+__global__ void __launch_bounds__(NT) k_proj_setup(const __grid_constant__ Dev D) {
   if (!(D.c[5] > .5)) return;
   Geo G(D, 2);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(NT) k_proj_setup(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 11 (gradient apply)
-__global__ void __launch_bounds__(NT) k_grad_apply(Dev D) {
+__global__ void __launch_bounds__(NT) k_grad_apply(const __grid_constant__ Dev D) {
   if (!post_on(D)) return;
   Geo G(D, 11);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(NT) k_grad_apply(Dev D) {
 }
 
 // ---------------------------------------------------------------- ops 30-33 (nearest sources)
-__global__ void __launch_bounds__(NT) k_ext_init(Dev D) {
+__global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) {
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(NT) k_ext_init(Dev D) {
   I3 l = ax(q, axis, -1);
   D.src0[f] = (!g.wall_face(q, axis) && (g.wet(q) || g.wet(l))) ? pack_face(q) : -1;
 }
-__global__ void __launch_bounds__(NT) k_ext_step(Dev D, int rb) {
+__global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, int rb) {
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -402,7 +402,7 @@ DI float extended_value(const Dev& D, const Grid& g, const float* Cb, int packed
 }
 
 // ---------------------------------------------------------------- op 34 + 47 + 48
-__global__ void __launch_bounds__(NT) k_ext_write(Dev D) {
+__global__ void __launch_bounds__(NT) k_ext_write(const __grid_constant__ Dev D) {
   if (!post_on(D)) return;
   Grid g(D);
   int cand = 1 - acc_bank(D);
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(NT) k_ext_write(Dev D) {
 }
 
 // ---------------------------------------------------------------- ops 35/36, 62/66, 65, 12/13
-__global__ void __launch_bounds__(NT) k_accept(Dev D) {
+__global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
   if (!post_on(D)) return;
   Geo G(D, 12);
   const Grid& g = G.g;
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(NT) k_accept(Dev D) {
 }
 
 // ---------------------------------------------------------------- ops 44, 85, 89 (one block)
-__global__ void __launch_bounds__(NT) k_trial_end(Dev D) {
+__global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D) {
   __shared__ float cols[8 * 128];
   Grid g(D);
   const float* A = bank_ptr(D, acc_bank(D));
@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(NT) k_trial_end(Dev D) {
 }
 
 // ---------------------------------------------------------------- coastal ops 80-84
-__global__ void __launch_bounds__(NT) k_coast_cells(Dev D) {
+__global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Geo G(D, 80);
   const Grid& g = G.g;
@@ -586,9 +586,9 @@ __global__ void __launch_bounds__(NT) k_coast_cells(Dev D) {
       long long i = g.index3(q);
       float time = (float)(D.c[1] + D.c[20]);
       F3 cq = g.center(q);
-      float old = G.Cb[i], rate = G.cs.rate(cq.x);
+      float old = G.Cb[i];
       float target = G.cs.offshore(cq.x) ? G.cs.fraction(g, q, time) : clampf_(.5f - cq.y / D.hy, 0.f, 1.f);
-      float value = old + (1.f - texp(-rate * G.dt)) * (target - old);
+      float value = old + G.cs.relax(g, q, -1, G.dt) * (target - old);
       G.Cb[i] = value;
       v[0] = ((double)value - (double)old) * D.cell_d;
       float vel[3];
@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(NT) k_coast_cells(Dev D) {
     D.c[69] += out[3];
   }
 }
-__global__ void __launch_bounds__(NT) k_coast_faces(Dev D) {
+__global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Geo G(D, 82);
   const Grid& g = G.g;
@@ -637,15 +637,15 @@ __global__ void __launch_bounds__(NT) k_coast_faces(Dev D) {
   F3 position = G.cs.face_position(g, q, axis);
   float old = G.Cb[D.N + f], value = old;
   if (!g.wall_face(q, axis)) {
-    float target = G.cs.offshore(position.x) ? G.cs.velocity_c(position, time, axis) : 0.f;
-    float a = 1.f - texp(-G.cs.rate(position.x) * G.dt);
+    float target = G.cs.offshore(position.x) ? G.cs.velocity_face(g, q, axis, time) : 0.f;
+    float a = G.cs.relax(g, q, axis, G.dt);
     value = old * (1.f - a) + target * a;
     if (axis == 0 && q.x == 0) value = target;
   }
   G.Cb[D.N + f] = value;
   D.fwd[f] = value - old;
 }
-__global__ void __launch_bounds__(NT) k_coast_momentum(Dev D) {
+__global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Geo G(D, 83);
   const Grid& g = G.g;
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(NT) k_coast_momentum(Dev D) {
 }
 
 // ---------------------------------------------------------------- export (op 19) into buffers
-__global__ void __launch_bounds__(NT) k_export(Dev D, float4* planes, float* kinds) {
+__global__ void __launch_bounds__(NT) k_export(const __grid_constant__ Dev D, float4* planes, float* kinds) {
   Geo G(D, 19);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;

@@ -9,7 +9,7 @@ namespace {
 constexpr int NT = 256;
 
 // op 0 (pressure_pass.glslinc:182-198)
-__global__ void __launch_bounds__(NT) k_init_still(Dev D) {
+__global__ void __launch_bounds__(NT) k_init_still(const __grid_constant__ Dev D) {
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.S) return;
@@ -42,7 +42,7 @@ DI float block_overlap(const Dev& D, F3 lo, F3 hi, F3 lower, F3 upper) {
   return o[0] * o[1] * o[2];
 }
 // op 40 (coupled_motion.glslinc:234-270)
-__global__ void __launch_bounds__(NT) k_init_fixture(Dev D) {
+__global__ void __launch_bounds__(NT) k_init_fixture(const __grid_constant__ Dev D) {
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   int shape = D.shape;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(NT) k_init_fixture(Dev D) {
 }
 
 // op 41/42
-__global__ void __launch_bounds__(NT) k_init_volume(Dev D) {
+__global__ void __launch_bounds__(NT) k_init_volume(const __grid_constant__ Dev D) {
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   double v[1] = {0};
   if (i < D.N) v[0] = (double)bank_ptr(D, acc_bank(D))[i] * D.cell_d;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(NT) k_init_volume(Dev D) {
 }
 
 // op 49 (coupled_motion.glslinc:323-337)
-__global__ void __launch_bounds__(NT) k_init_masks(Dev D) {
+__global__ void __launch_bounds__(NT) k_init_masks(const __grid_constant__ Dev D) {
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i < D.N) {
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(NT) k_init_masks(Dev D) {
 }
 
 // op 86 (coastal_pass.glslinc:78-83)
-__global__ void k_probes(Dev D, float4* out) {
+__global__ void k_probes(const __grid_constant__ Dev D, float4* out) {
   int i = threadIdx.x;
   if (i >= 8) return;
   Coast cs(D);

@@ -7,6 +7,8 @@
 // each thread of a group (the children of I in one (y, z) fine row) accumulates
 // (a_ij * w_iI) * w_jJ into its own shared-memory row of 125 slots, and the row is the sum of the
 // group partials in group order.  No float atomics touch any result.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -29,7 +31,6 @@ DI int pmod(int x, int m) { return pidx(x, m); }
 struct MG {
   const Dev& D;
   DI explicit MG(const Dev& d) : D(d) {}
-  DI const MGLevelDev& L(int l) const { return D.lv[l]; }
   DI int wrap(int l, I3 q) const {
     const MGLevelDev& v = D.lv[l];
     q.z = pmod(q.z, v.nz);
@@ -129,8 +130,9 @@ struct MG {
     }
     return size;
   }
-  // apply (pressure_multigrid.glslinc:90-105) with the V-cycle operators
-  template <class T> DI float apply(int l, int f, int i) const {
+  // apply (pressure_multigrid.glslinc:90-105) with the V-cycle operators; `lin_s` (optional) is a
+  // copy of the level's linear stencil offsets in shared memory.
+  template <class T> DI float apply(int l, int f, int i, const int* lin_s = nullptr) const {
     const T* x = field<T>(f, l);
     if (!active<T>(l, i)) return ld_val(x[i]);
     float sum = 0.f;
@@ -151,6 +153,11 @@ struct MG {
     const T* ell = (const T*)D.mgell + lv.eoff;
     if (q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2) {
       // every stencil point is inside: the neighbour is i + linear offset, no wrap
+      if (lin_s) {
+#pragma unroll 13
+        for (int k = 0; k < lv.stencil; k++) sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[i + lin_s[k]]);
+        return sum;
+      }
       const int* lin = D.stencil_lin + lv.soff;
 #pragma unroll 8
       for (int k = 0; k < lv.stencil; k++) sum += ld_val(ell[(long long)k * lv.count + i]) * ld_val(x[i + __ldg(lin + k)]);
@@ -182,7 +189,7 @@ DI unsigned signature(const Dev& D, const Grid& g, long long i) {
     }
   return result;
 }
-__global__ void k_hs_reset(Dev D) {
+__global__ void k_hs_reset(const __grid_constant__ Dev D) {
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   for (int k = 1; k <= 7; k++) s[k] = 0;
@@ -193,7 +200,7 @@ __global__ void k_hs_reset(Dev D) {
 }
 struct AddU { DI unsigned operator()(unsigned a, unsigned b) const { return a + b; } };
 struct MaxU { DI unsigned operator()(unsigned a, unsigned b) const { return a < b ? b : a; } };
-__global__ void __launch_bounds__(NT) k_hs_count(Dev D) {
+__global__ void __launch_bounds__(NT) k_hs_count(const __grid_constant__ Dev D) {
   if (!build_on(D)) return;
   __shared__ unsigned sh[32];
   Grid g(D);
@@ -237,7 +244,7 @@ __global__ void __launch_bounds__(NT) k_hs_count(Dev D) {
     }
   }
 }
-__global__ void k_hs_decide(Dev D) {
+__global__ void k_hs_decide(const __grid_constant__ Dev D) {
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   double* c = D.c;
@@ -260,7 +267,7 @@ __global__ void k_hs_decide(Dev D) {
     s[row + 9] = s[8]; s[row + 10] = s[9]; s[row + 11] = s[10]; s[row + 12] = s[16]; s[row + 13] = s[11];
   }
 }
-template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(Dev D) {
+template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(const __grid_constant__ Dev D) {
   if (!build_on(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -283,7 +290,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(Dev D) {
     }
   }
 }
-__global__ void k_hs_record(Dev D) {
+__global__ void k_hs_record(const __grid_constant__ Dev D) {
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   if (s[13] <= (unsigned)D.hist_cap) {
@@ -293,7 +300,7 @@ __global__ void k_hs_record(Dev D) {
 }
 
 // ---------------------------------------------------------------- build ops
-template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(Dev D, int l) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_constant__ Dev D, int l) {
   if (!build_on(D) || D.hstate[9] == 0) return;
   __shared__ unsigned sh[32];
   MG m(D);
@@ -319,7 +326,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(Dev D, int l)
   unsigned r = block_reduce<NT>(changed, AddU(), sh);
   if (threadIdx.x == 0 && r) atomicAdd(&D.hstate[20 + l], r);
 }
-template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(Dev D, int l) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __grid_constant__ Dev D, int l) {
   if (!build_on(D) || !(D.hstate[14] == 0 || D.hstate[20 + l + 1] != 0)) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -334,7 +341,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(Dev D, in
   }
 }
 // l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(Dev D, int l) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(const __grid_constant__ Dev D, int l) {
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -372,7 +379,7 @@ DI void child_range(const Dev& D, int l, int axis, int qc, int& lo, int& ext) {
   if (periodic && nf <= 4) { lo = 0; ext = nf; }
 }
 // Deterministic Galerkin product of level l into level l+1 (replaces ops 2 + 3).
-template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(Dev D, int l, int ex, int ey, int ez) {
+template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __grid_constant__ Dev D, int l, int ex, int ey, int ez) {
   if (!build_on(D) || D.hstate[8] == 0) return;
   extern __shared__ float part[];  // [125][GT]
   MG m(D);
@@ -432,7 +439,7 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(Dev D, in
   }
 }
 // ELL rows (pressure_multigrid.glslinc:176-182)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(Dev D, int l) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_constant__ Dev D, int l) {
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -448,7 +455,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(Dev D, int l) 
   }
 }
 // Dense Cholesky and L^-1 of the last level (pressure_mg_coarse.glslinc:34-48), one block.
-template <class T> __global__ void k_mg_chol(Dev D, int l) {
+template <class T> __global__ void k_mg_chol(const __grid_constant__ Dev D, int l) {
   if (!build_on(D) || D.hstate[8] == 0) return;
   __shared__ float dense[64 * 64];
   __shared__ float inv[64 * 64];
@@ -487,43 +494,92 @@ template <class T> __global__ void k_mg_chol(Dev D, int l) {
 }
 
 // ---------------------------------------------------------------- V-cycle
-// Per-cell operations, shared by the grid kernels and by the single-block bottom solver.
-template <class T> DI void cheb_cell(const MG& m, int l, int source, int k, int i, bool src_zero) {
+// Per-cell operations, shared by the grid kernels and by the single-block bottom solver.  `ax`
+// is apply(l, source, i) of the cell (unused where the update needs no operator).
+template <class T, class M> DI void cheb_update(const M& m, int l, int source, int k, int i, bool src_zero, float ax) {
   float c1 = (float)(2 * k - 3) / (float)(2 * k + 1), c2 = (float)(8 * k - 4) / (float)(2 * k + 1);
-  const T* x = m.field<T>(source, l);
+  const T* x = m.template field<T>(source, l);
   // A zero iterate makes apply() exactly +0, so r = b exactly; skip the operator.
-  float r = src_zero ? ld_val(m.field<T>(0, l)[i]) : ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, source, i);
-  T* v7 = m.field<T>(7, l);
-  float d = (k == 1 ? 0.f : c1 * ld_val(v7[i])) + c2 * ld_val(m.field<T>(4, l)[i]) * r;
+  float r = src_zero ? ld_val(m.template field<T>(0, l)[i]) : ld_val(m.template field<T>(0, l)[i]) - ax;
+  T* v7 = m.template field<T>(7, l);
+  float d = (k == 1 ? 0.f : c1 * ld_val(v7[i])) + c2 * ld_val(m.template field<T>(4, l)[i]) * r;
   float xv = (src_zero ? 0.f : ld_val(x[i])) + d;
   v7[i] = st_val<T>(d);
-  m.field<T>(3 - source, l)[i] = st_val<T>(xv);
+  m.template field<T>(3 - source, l)[i] = st_val<T>(xv);
 }
-template <class T> DI void jacobi_cell(const MG& m, int l, int source, int first, int i) {
-  float s = ld_val(m.field<T>(4, l)[i]), b = ld_val(m.field<T>(0, l)[i]);
-  if (first) m.field<T>(2, l)[i] = st_val<T>(s * b);
-  else m.field<T>(3 - source, l)[i] = st_val<T>(ld_val(m.field<T>(source, l)[i]) + s * (b - m.apply<T>(l, source, i)));
+template <class T, class M> DI void jacobi_update(const M& m, int l, int source, int first, int i, float ax) {
+  float s = ld_val(m.template field<T>(4, l)[i]), b = ld_val(m.template field<T>(0, l)[i]);
+  if (first) m.template field<T>(2, l)[i] = st_val<T>(s * b);
+  else m.template field<T>(3 - source, l)[i] = st_val<T>(ld_val(m.template field<T>(source, l)[i]) + s * (b - ax));
 }
-template <class T> DI void residual_cell(const MG& m, int l, int f, int i) {
-  m.field<T>(6, l)[i] = st_val<T>(ld_val(m.field<T>(0, l)[i]) - m.apply<T>(l, f, i));
+template <class T, class M> DI void residual_update(const M& m, int l, int i, float ax) {
+  m.template field<T>(6, l)[i] = st_val<T>(ld_val(m.template field<T>(0, l)[i]) - ax);
 }
+template <class T, class M> DI void cheb_cell(const M& m, int l, int source, int k, int i, bool src_zero) {
+  cheb_update<T>(m, l, source, k, i, src_zero, src_zero ? 0.f : m.template apply<T>(l, source, i));
+}
+template <class T, class M> DI void jacobi_cell(const M& m, int l, int source, int first, int i) {
+  jacobi_update<T>(m, l, source, first, i, first ? 0.f : m.template apply<T>(l, source, i));
+}
+template <class T, class M> DI void residual_cell(const M& m, int l, int f, int i) { residual_update<T>(m, l, i, m.template apply<T>(l, f, i)); }
+
+// Product-parallel apply for levels >= 1: the whole block computes the products
+// ell[k][i] * x[col(k, i)] of RR consecutive rows into shared memory (every load independent),
+// then one thread per row adds its products in stencil order k = 0, 1, ... -- the same roundings
+// and the same order as apply(), so the value is bit-identical.
+constexpr int RR = 32;
+template <class T> DI void row_products(const MG& m, int l, int src, int row0, float* prod, bool* inner, int* lin) {
+  const Dev& D = m.D;
+  const MGLevelDev& lv = D.lv[l];
+  const int S = lv.stencil, n = lv.count;
+  if (threadIdx.x < RR) {
+    int i = row0 + threadIdx.x;
+    I3 q = m.coord(l, i < n ? i : 0);
+    inner[threadIdx.x] = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
+  }
+  for (int k = threadIdx.x; k < S; k += NT) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
+  __syncthreads();
+  const T* x = m.field<T>(src, l);
+  const T* ell = (const T*)D.mgell + lv.eoff;
+  const int* col = D.mgcol + lv.eoff;
+#pragma unroll 4
+  for (int p = threadIdx.x; p < S * RR; p += NT) {
+    const int k = p / RR, r = p % RR, i = row0 + r;
+    float v = 0.f;
+    if (i < n) {
+      const long long e = (long long)k * n + i;
+      const int j = inner[r] ? i + lin[k] : __ldg(col + e);
+      v = ld_val(ell[e]) * ld_val(x[j]);
+    }
+    prod[p] = v;
+  }
+  __syncthreads();
+}
+template <class T> DI float row_sum(const MG& m, int l, int src, int i, const float* prod) {
+  if (!m.active<T>(l, i)) return ld_val(m.field<T>(src, l)[i]);
+  const int S = m.D.lv[l].stencil;
+  float sum = 0.f;
+  for (int k = 0; k < S; k++) sum += prod[k * RR + threadIdx.x];
+  return sum;
+}
+
 // op 8: exact P^T restriction into coarse level l (pressure_multigrid.glslinc:200-224); the
 // per-axis weights come from the tables built with the same arithmetic at set-up.
-template <class T> DI void restrict_cell(const MG& m, int l, int i) {
+template <class T, class M> DI void restrict_cell(const M& m, int l, int i) {
   const Dev& D = m.D;
   const MGLevelDev& cv = D.lv[l];
   const int parent = l - 1;
   const MGLevelDev& pv = D.lv[parent];
-  const T* r6 = m.field<T>(6, parent);
+  const T* r6 = m.template field<T>(6, parent);
   float sum = 0.f;
   I3 qc = m.coord(l, i);
-  if (m.active<T>(l, i)) {
+  if (m.template active<T>(l, i)) {
     if (pv.aggregate) {
       for (int z = 0; z < pv.fz; z++)
         for (int y = 0; y < pv.fy; y++)
           for (int x = 0; x < pv.fx; x++) {
             int j = m.wrap(parent, mk(qc.x * pv.fx + x, qc.y * pv.fy + y, qc.z * pv.fz + z));
-            if (m.active<T>(parent, j)) sum += ld_val(r6[j]);
+            if (m.template active<T>(parent, j)) sum += ld_val(r6[j]);
           }
     } else {
       const int* ix = D.rt_idx + cv.roff[0] + 4 * qc.x;
@@ -540,34 +596,36 @@ template <class T> DI void restrict_cell(const MG& m, int l, int i) {
             int fx = ix[tx];
             if (fx < 0) continue;
             int j = fx + pv.nx * (fy + pv.ny * iz[tz]);
-            if (!m.active<T>(parent, j)) continue;
+            if (!m.template active<T>(parent, j)) continue;
             float weight = 1.f * wx[tx] * wy[ty] * wz[tz];
             sum += weight * ld_val(r6[j]);
           }
         }
     }
   }
-  m.field<T>(0, l)[i] = st_val<T>(sum);
-  m.field<T>(1, l)[i] = st_val<T>(0.f);
-  m.field<T>(2, l)[i] = st_val<T>(0.f);
+  m.template field<T>(0, l)[i] = st_val<T>(sum);
+  m.template field<T>(1, l)[i] = st_val<T>(0.f);
+  m.template field<T>(2, l)[i] = st_val<T>(0.f);
 }
-template <class T> DI void prolong_cell(const MG& m, int l, int ff, int cf, int i) {
+template <class T, class M> DI void prolong_cell(const M& m, int l, int ff, int cf, int i) {
   float add = 0.f;
-  if (m.active<T>(l, i)) {
+  if (m.template active<T>(l, i)) {
     int ids[8];
     float ws[8];
-    int size = m.transfers(l, i, ids, ws);
-    const T* xc = m.field<T>(cf, l + 1);
+    // The stored transfers are compute_transfers() on the current coarse mask (rebuilt whenever
+    // that mask changes); at level 0 recomputing them is cheaper than reading the table.
+    int size = l == 0 ? m.template compute_transfers<T>(l, i, ids, ws) : m.transfers(l, i, ids, ws);
+    const T* xc = m.template field<T>(cf, l + 1);
     for (int k = 0; k < size; k++) add += ws[k] * ld_val(xc[ids[k]]);
   }
-  T* x = m.field<T>(ff, l);
+  T* x = m.template field<T>(ff, l);
   x[i] = st_val<T>(ld_val(x[i]) + add);
 }
 // op 12: x = L^-T (L^-1 b), threads 0..n-1 of one block
-template <class T> DI void coarse_block(const MG& m, int l, float* small) {
+template <class T, class M> DI void coarse_block(const M& m, int l, float* small) {
   const Dev& D = m.D;
   const int n = D.lv[l].count, t = threadIdx.x;
-  const T* b = m.field<T>(0, l);
+  const T* b = m.template field<T>(0, l);
   if (t < n) {
     float d = 0.f;
     for (int j = 0; j <= t; j++) d += D.mglinv[t * n + j] * ld_val(b[j]);
@@ -577,69 +635,83 @@ template <class T> DI void coarse_block(const MG& m, int l, float* small) {
   if (t < n) {
     float d = 0.f;
     for (int j = t; j < n; j++) d += D.mglinv[j * n + t] * small[j];
-    m.field<T>(1, l)[t] = st_val<T>(d);
+    m.template field<T>(1, l)[t] = st_val<T>(d);
   }
   __syncthreads();
 }
 
-// Level 0: 3-D thread mapping (x threads, y and z blocks), the neighbour-active bits of mgnb0.
+// Level 0: each 256-thread block covers a 32 (x) by 8 (y) tile of one z plane, so a warp reads
+// 128 contiguous bytes of every field; mgnb0 holds the neighbour-active bits.  Indices are 32-bit
+// (level 0 holds fewer than 2^31 cells).
+constexpr int kTileX = 32, kTileY = NT / kTileX;
 struct Cell0 {
-  int x, y, z;
-  long long i;
+  int x, y, z, i;
   bool ok;
 };
 DI Cell0 cell0(const Dev& D) {
   Cell0 c;
-  c.x = blockIdx.x * blockDim.x + threadIdx.x;
-  c.y = blockIdx.y;
+  c.x = blockIdx.x * kTileX + (threadIdx.x & (kTileX - 1));
+  c.y = blockIdx.y * kTileY + threadIdx.x / kTileX;
   c.z = blockIdx.z;
-  c.ok = c.x < D.nx;
-  c.i = (long long)(c.ok ? c.x : 0) + (long long)D.nx * ((long long)c.y + (long long)D.ny * c.z);
+  c.ok = c.x < D.nx && c.y < D.ny;
+  c.i = c.ok ? c.x + D.nx * (c.y + D.ny * c.z) : 0;
   return c;
 }
+template <class T> DI T* field0(const Dev& D, int f) { return (T*)D.mgv + (size_t)f * (size_t)D.mg_nodes; }
 // apply at level 0 (pressure_multigrid.glslinc:93-99) with neighbour activity from one byte.
-template <class T> DI float apply0(const Dev& D, const T* x, const Cell0& c) {
-  unsigned m = D.mgnb0[c.i];
-  if (!(m & 64u)) return ld_val(x[c.i]);
-  const T* c0 = (const T*)D.c0;
-  const long long plane = (long long)D.nx * D.ny, N = D.N;
-  long long nb[6];
-  nb[0] = c.x > 0 ? c.i - 1 : c.i + (D.nx - 1);
-  nb[1] = c.x < D.nx - 1 ? c.i + 1 : c.i - (D.nx - 1);
-  nb[2] = c.i - D.nx;
-  nb[3] = c.i + D.nx;
+// Every load is issued before the activity bits are known: neighbour indices are clamped to the
+// cell itself where no neighbour exists, and a value whose bit is clear is replaced by zero.
+template <class T> DI float apply0(const Dev& D, const T* __restrict__ x, const Cell0& c) {
+  const T* __restrict__ c0 = (const T*)D.c0;
+  const int nx = D.nx, plane = D.nx * D.ny, N = (int)D.N;
+  int nb[6];
+  nb[0] = c.x > 0 ? c.i - 1 : c.i + (nx - 1);
+  nb[1] = c.x < nx - 1 ? c.i + 1 : c.i - (nx - 1);
+  nb[2] = c.y > 0 ? c.i - nx : c.i;
+  nb[3] = c.y < D.ny - 1 ? c.i + nx : c.i;
   nb[4] = c.z > 0 ? c.i - plane : c.i + plane * (D.nz - 1);
   nb[5] = c.z < D.nz - 1 ? c.i + plane : c.i - plane * (D.nz - 1);
-  float here = ld_val(x[c.i]);
+  const unsigned m = D.mgnb0[c.i];
+  const float here = ld_val(x[c.i]);
+  float xo[6], kf[6];
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    xo[f] = ld_val(x[nb[f]]);
+    kf[f] = ld_val(c0[f * N + c.i]);
+  }
+  if (!(m & 64u)) return here;
   float sum = 0.f;
 #pragma unroll
   for (int f = 0; f < 6; f++) {
-    float other = (m >> f) & 1u ? ld_val(x[nb[f]]) : 0.f;
-    sum += ld_val(c0[(long long)f * N + c.i]) * (here - other);
+    float other = (m >> f) & 1u ? xo[f] : 0.f;
+    sum += kf[f] * (here - other);
   }
   return sum;
 }
-// Chebyshev sweep k at level 0; with fin >= 0 it is the last post-smoothing sweep and also does
-// op 10 of the cycle (z, partial sums) and the op 4 (phase 0) / op 9 (phase 1) finalisation.
-template <class T> __global__ void __launch_bounds__(NT) k_mg0_cheb(Dev D, int phase, int source, int k, int src_zero, int fin) {
+// Chebyshev sweep k at level 0 (coefficients c1 = (2k-3)/(2k+1), c2 = (8k-4)/(2k+1), rounded to
+// float by the caller); with fin >= 0 it is the last post-smoothing sweep and also does op 10 of
+// the cycle (z, partial sums) and the op 4 (phase 0) / op 9 (phase 1) finalisation.
+template <class T>
+__global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, int phase, int source, float c1, float c2,
+                                                  int first_k, int src_zero, int fin) {
   if (!phase_on(D, phase)) return;
-  Cell0 c = cell0(D);
-  MG m(D);
-  float c1 = (float)(2 * k - 3) / (float)(2 * k + 1), c2 = (float)(8 * k - 4) / (float)(2 * k + 1);
+  const Cell0 c = cell0(D);
   double v[4] = {0, 0, 0, 0};
   if (c.ok) {
-    const T* x = m.field<T>(source, 0);
-    float b = ld_val(m.field<T>(0, 0)[c.i]);
-    float r = src_zero ? b : b - apply0<T>(D, x, c);
-    T* v7 = m.field<T>(7, 0);
-    float d = (k == 1 ? 0.f : c1 * ld_val(v7[c.i])) + c2 * ld_val(m.field<T>(4, 0)[c.i]) * r;
-    float xv = (src_zero ? 0.f : ld_val(x[c.i])) + d;
-    T xs = st_val<T>(xv);
+    const T* __restrict__ x = field0<T>(D, source);
+    T* v7 = field0<T>(D, 7);
+    const float b = ld_val(field0<T>(D, 0)[c.i]);
+    const float sc = ld_val(field0<T>(D, 4)[c.i]);
+    const float dprev = first_k ? 0.f : ld_val(v7[c.i]);
+    const float r = src_zero ? b : b - apply0<T>(D, x, c);
+    const float d = (first_k ? 0.f : c1 * dprev) + c2 * sc * r;
+    const float xv = (src_zero ? 0.f : ld_val(x[c.i])) + d;
+    const T xs = st_val<T>(xv);
     if (fin < 0) {
       v7[c.i] = st_val<T>(d);
-      m.field<T>(3 - source, 0)[c.i] = xs;
+      field0<T>(D, 3 - source)[c.i] = xs;
     } else {
-      float rr = D.r[c.i], z = ld_val(xs), bb = D.b[c.i];
+      const float rr = D.r[c.i], z = ld_val(xs), bb = D.b[c.i];
       D.z[c.i] = z;
       if (phase == 0) D.d[c.i] = z;
       v[0] = (double)rr * (double)z;
@@ -656,15 +728,14 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_cheb(Dev D, int p
     else finalize_op9(D, out);
   }
 }
-template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(Dev D, int phase, int f) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __grid_constant__ Dev D, int phase, int f) {
   if (!phase_on(D, phase)) return;
-  Cell0 c = cell0(D);
+  const Cell0 c = cell0(D);
   if (!c.ok) return;
-  MG m(D);
-  m.field<T>(6, 0)[c.i] = st_val<T>(ld_val(m.field<T>(0, 0)[c.i]) - apply0<T>(D, m.field<T>(f, 0), c));
+  field0<T>(D, 6)[c.i] = st_val<T>(ld_val(field0<T>(D, 0)[c.i]) - apply0<T>(D, field0<T>(D, f), c));
 }
 // phase 0 load (op 5 of the cycle) fused with the first Chebyshev sweep from zero
-template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(Dev D, int phase, int first_sweep) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid_constant__ Dev D, int phase, int first_sweep) {
   if (!phase_on(D, phase)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -683,23 +754,52 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(Dev D, int p
 }
 
 // Generic levels (l >= 1): one thread per cell.
-template <class T> __global__ void __launch_bounds__(NT) k_mgl(Dev D, int phase, int op, int l, int a, int b, int c) {
+template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   if (!phase_on(D, phase)) return;
+  __shared__ int lin[kMaxStencil];
+  const int* lin_s = nullptr;
+  if (op <= 2 && l >= 1) {
+    for (int k = threadIdx.x; k < D.lv[l].stencil; k += NT) lin[k] = __ldg(D.stencil_lin + D.lv[l].soff + k);
+    __syncthreads();
+    lin_s = lin;
+  }
   int i = blockIdx.x * NT + threadIdx.x;
   if (i >= D.lv[l].count) return;
   MG m(D);
   switch (op) {
-    case 0: cheb_cell<T>(m, l, a, b, i, c != 0); break;
-    case 1: jacobi_cell<T>(m, l, a, b, i); break;
-    case 2: residual_cell<T>(m, l, a, i); break;
+    case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : m.apply<T>(l, a, i, lin_s)); break;
+    case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : m.apply<T>(l, a, i, lin_s)); break;
+    case 2: residual_update<T>(m, l, i, m.apply<T>(l, a, i, lin_s)); break;
     case 3: restrict_cell<T>(m, l, i); break;
     case 4: prolong_cell<T>(m, l, a, b, i); break;
   }
 }
 
+// Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a level >= 1 with the
+// product-parallel apply: RR rows per block.
+template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+  if (!phase_on(D, phase)) return;
+  __shared__ float prod[kMaxStencil * RR];
+  __shared__ bool inner[RR];
+  __shared__ int lin[kMaxStencil];
+  MG m(D);
+  const int row0 = blockIdx.x * RR;
+  const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);
+  if (need) row_products<T>(m, l, a, row0, prod, inner, lin);
+  if (threadIdx.x >= RR) return;
+  const int i = row0 + threadIdx.x;
+  if (i >= D.lv[l].count) return;
+  const float ax = need ? row_sum<T>(m, l, a, i, prod) : 0.f;
+  switch (op) {
+    case 0: cheb_update<T>(m, l, a, b, i, c != 0, ax); break;
+    case 1: jacobi_update<T>(m, l, a, b, i, ax); break;
+    case 2: residual_update<T>(m, l, i, ax); break;
+  }
+}
+
 // Whole sub-cycle from level lb down to the coarsest and back, in one block.
 // Returns (in *out_field) the field holding the level-lb correction.
-template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(Dev D, int phase, int lb) {
+template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __grid_constant__ Dev D, int phase, int lb) {
   if (!phase_on(D, phase)) return;
   __shared__ float small[64];
   MG m(D);
@@ -745,7 +845,7 @@ template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(Dev D, in
 }
 
 // op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(Dev D, int phase, int f) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __grid_constant__ Dev D, int phase, int f) {
   if (!phase_on(D, phase)) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -769,12 +869,51 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(Dev D, int 
 
 unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
 
+// Algorithmic bytes of one level >= 1 sweep (op 0 Chebyshev, 1 Jacobi, 2 residual): with the
+// operator, the row values and columns of rows that wrap, the source iterate and the activity
+// field; then the op's own vectors.  tb = storage bytes of a multigrid value.
+// Chebyshev coefficients of sweep k (pressure_multigrid.glslinc:206-207), correctly rounded
+// float quotients exactly as the device computes them in cheb_update.
+float cheb_c1(int k) { return (float)(2 * k - 3) / (float)(2 * k + 1); }
+float cheb_c2(int k) { return (float)(8 * k - 4) / (float)(2 * k + 1); }
+
+double level_op_bytes(const Dev& D, int l, int op, int b, int c, double tb) {
+  const MGLevelDev& v = D.lv[l];
+  const double n = v.count;
+  const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);
+  const double inner = (double)std::max(0, v.nx - 4) * std::max(0, v.ny - 4) * std::max(0, v.nz - 4);
+  double bytes = need ? n * v.stencil * tb + 2.0 * n * tb + (n - inner) * v.stencil * 4.0 : 0.0;
+  if (op == 0) bytes += n * tb * ((b > 1 ? 1.0 : 0.0) + 2.0 + 2.0);  // d_prev, b, scale; d, x
+  else if (op == 1) bytes += 3.0 * n * tb;                            // scale, b; x
+  else bytes += 2.0 * n * tb;                                         // b; residual
+  return bytes;
+}
+// Level-0 Chebyshev sweep: activity byte, six coefficients, b and scale, the iterate unless it is
+// zero, d_prev after the first sweep; writes d and x, or (last sweep) reads r, b and writes z (and d).
+double smooth0_bytes(const Dev& D, int phase, int k, int src_zero, int fin, double tb) {
+  const double n = (double)D.N;
+  double bytes = n * (1.0 + tb * (8.0 + (src_zero ? 0.0 : 1.0) + (k > 1 ? 1.0 : 0.0)));
+  bytes += fin < 0 ? 2.0 * n * tb : n * (8.0 + 4.0 + (phase == 0 ? 4.0 : 0.0));
+  return bytes;
+}
+
 template <class T> struct Cycle {
   const Dev& D;
   cudaStream_t s;
   int phase;
   int fused_first;  // the level-0 first pre-smoothing sweep was done by the caller
-  dim3 grid0() const { return dim3((unsigned)((D.nx + NT - 1) / NT), (unsigned)D.ny, (unsigned)D.nz); }
+  unsigned rows_grid(int l) const { return (unsigned)((D.lv[l].count + RR - 1) / RR); }
+  // Levels with few rows use the product-parallel kernel (enough independent loads in flight);
+  // larger levels keep one thread per row.
+  bool few_rows(int l) const { return D.lv[l].count < D.mg_rows_below; }
+  void level_op(int l, int op, int a, int b, int c) {
+    const double bytes = level_op_bytes(D, l, op, b, c, sizeof(T));
+    if (few_rows(l))
+      probed(kProbeRows, s, bytes, [&] { k_mgl_rows<T><<<rows_grid(l), NT, 0, s>>>(D, phase, op, l, a, b, c); });
+    else
+      probed(kProbeRowThread, s, bytes, [&] { k_mgl<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, phase, op, l, a, b, c); });
+  }
+  dim3 grid0() const { return dim3((unsigned)((D.nx + kTileX - 1) / kTileX), (unsigned)((D.ny + kTileY - 1) / kTileY), (unsigned)D.nz); }
   int smooth(int l, int field, bool zero, bool last0) {
     unsigned gr = grid_for(D.lv[l].count);
     for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
@@ -785,10 +924,16 @@ template <class T> struct Cycle {
         continue;
       }
       if (D.mg_smoother == 1) {
-        if (l == 0) k_mg0_cheb<T><<<grid0(), NT, 0, s>>>(D, phase, field, sweep + 1, first ? 1 : 0, fin ? 1 : -1);
-        else k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 0, l, field, sweep + 1, first ? 1 : 0);
-      } else
+        if (l == 0)
+          probed(kProbeSmooth0, s, smooth0_bytes(D, phase, sweep + 1, first ? 1 : 0, fin ? 1 : -1, sizeof(T)), [&] {
+            k_mg0_cheb<T><<<grid0(), NT, 0, s>>>(D, phase, field, cheb_c1(sweep + 1), cheb_c2(sweep + 1), sweep == 0 ? 1 : 0,
+                                                 first ? 1 : 0, fin ? 1 : -1);
+          });
+        else level_op(l, 0, field, sweep + 1, first ? 1 : 0);
+      } else if (l == 0)
         k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 1, l, field, first ? 1 : 0, 0);
+      else
+        level_op(l, 1, field, first ? 1 : 0, 0);
       field = 3 - field;
     }
     return field;
@@ -807,7 +952,7 @@ template <class T> struct Cycle {
     }
     int field = smooth(l, 1, true, false);
     if (l == 0) k_mg0_residual<T><<<grid0(), NT, 0, s>>>(D, phase, field);
-    else k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 2, l, field, 0, 0);
+    else level_op(l, 2, field, 0, 0);
     k_mgl<T><<<grid_for(D.lv[l + 1].count), NT, 0, s>>>(D, phase, 3, l + 1, 0, 0, 0);
     int cf = level(l + 1);
     k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 4, l, field, cf, 0);
@@ -823,7 +968,7 @@ template <class T> struct Cycle {
 };
 
 // Columns of the ELL rows, max(wrap(l, q + offset), 0), computed once (static geometry).
-__global__ void __launch_bounds__(NT) k_mg_cols(Dev D, int l) {
+__global__ void __launch_bounds__(NT) k_mg_cols(const __grid_constant__ Dev D, int l) {
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
   int i = blockIdx.x * NT + threadIdx.x;
@@ -837,7 +982,7 @@ __global__ void __launch_bounds__(NT) k_mg_cols(Dev D, int l) {
 
 // Level-0 neighbour-active bits (bit f: neighbour across face f active, bit 6: cell active),
 // rebuilt after the masks on structural rebuilds.
-template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(Dev D) {
+template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(const __grid_constant__ Dev D) {
   if (!build_on(D) || D.hstate[9] == 0) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;

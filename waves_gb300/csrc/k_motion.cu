@@ -29,7 +29,7 @@ struct Motion {
   // old_face (coupled_motion.glslinc:28-35)
   DI float old_face(I3 q, int axis) const {
     q = g.wrap_face(q);
-    if (D.coastal && q.x < 0 && !g.wall_face(q, axis)) return cs.velocity_c(cs.face_position(g, q, axis), (float)c1, axis);
+    if (D.coastal && q.x < 0 && !g.wall_face(q, axis)) return cs.velocity_face(g, q, axis, (float)c1);
     if (!g.face_in_bounds(q, axis) || g.wall_face(q, axis)) return 0.f;
     return A[g.face_index(q, axis)];
   }
@@ -55,12 +55,11 @@ struct Motion {
       float tt = (float)(c1 + (double)D.dtcfg);
       if (cs.rate(cq.x) > 0.f) {
         float s0, s1;
-        cs.surface(cq.x, tt, s0, s1);
+        cs.surface_col(g, q.x, tt, s0, s1);
         if (cq.y < s0 + 3.f * D.hy) {
           for (int axis = 0; axis < 3; axis++) {
             I3 r = ax(q, axis, 1);
-            s[axis] = mxf(s[axis], mxf(fabsf(cs.velocity_c(cs.face_position(g, q, axis), tt, axis)),
-                                       fabsf(cs.velocity_c(cs.face_position(g, r, axis), tt, axis))));
+            s[axis] = mxf(s[axis], mxf(fabsf(cs.velocity_face(g, q, axis, tt)), fabsf(cs.velocity_face(g, r, axis, tt))));
           }
         }
       }
@@ -75,8 +74,39 @@ struct Motion {
 
 DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
 
+// ---------------------------------------------------------------- wave-target tables
+// which 0: the accepted time and the CFL look-ahead time (before op 20); which 1: the new time
+// c1 + dt and the relaxation factors at dt (after op 20 has set dt).  One thread per (column, row).
+__global__ void __launch_bounds__(NT) k_wave_tables(const __grid_constant__ Dev D, int which) {
+  if (!setup_on(D)) return;
+  const Grid g(D);
+  const Coast cs(D);
+  const int t = blockIdx.x * NT + threadIdx.x;
+  if (t >= D.wt_w * D.wt_h) return;
+  const int j = t % D.wt_w, y = t / D.wt_w, x = D.wt_x0 + j;
+  const double c1 = D.c[1];
+  const float times[3] = {(float)c1, (float)(c1 + (double)D.dtcfg), (float)(c1 + D.c[20])};
+  for (int sl = which == 0 ? 0 : 2; sl <= (which == 0 ? 1 : 2); sl++) {
+    const float time = times[sl];
+    if (y == 0) {
+      float s0, s1;
+      cs.surface(g.center(mk(x, 0, 0)).x, time, s0, s1);
+      D.wsurf[sl * D.wt_w + j] = make_float2(s0, s1);
+    }
+    for (int axis = 0; axis < 2; axis++)
+      D.wvel[((sl * 2 + axis) * D.wt_h + y) * D.wt_w + j] = cs.velocity_c(cs.face_position(g, mk(x, y, 0), axis), time, axis);
+    if (t == 0) D.wstamp[sl] = time;
+  }
+  if (which == 1 && y == 0) {
+    const float dt = (float)D.c[20];
+    D.wdecay[j] = 1.f - texp(-cs.rate(g.center(mk(x, 0, 0)).x) * dt);
+    D.wdecay[D.wt_w + j] = 1.f - texp(-cs.rate(cs.face_position(g, mk(x, 0, 0), 0).x) * dt);
+    if (t == 0) D.wstamp[3] = dt;
+  }
+}
+
 // ---------------------------------------------------------------- op 20/21
-__global__ void __launch_bounds__(NT) k_cfl(Dev D) {
+__global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -97,7 +127,7 @@ __global__ void __launch_bounds__(NT) k_cfl(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 45/46 + c_i of op 22
-__global__ void __launch_bounds__(NT) k_compress(Dev D) {
+__global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Motion m(D);
   const float* pmA = m.acc == 0 ? D.pmask0 : D.pmask1;
@@ -129,7 +159,7 @@ __global__ void __launch_bounds__(NT) k_compress(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 23
-__global__ void __launch_bounds__(NT) k_sweep_plane(Dev D) {
+__global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -169,7 +199,7 @@ DI float sweep_flux(const Motion& m, I3 q, int axis) {
 }
 
 // ---------------------------------------------------------------- op 24 + 55/56 + 25/26
-__global__ void __launch_bounds__(NT) k_sweep_update(Dev D) {
+__global__ void __launch_bounds__(NT) k_sweep_update(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Motion m(D);
   int sa = ((int)D.c[2] + (int)D.c[21]) % 3;
@@ -278,7 +308,7 @@ struct Mac {
     q = g.wrap_face(q);
     if (D.coastal && q.x < 0 && q.y >= 0 && q.y < D.ny && !g.wall_face(q, axis)) {
       valid = true;
-      return parity * m.cs.velocity_c(m.cs.face_position(g, q, axis), (float)m.c1, axis);
+      return parity * m.cs.velocity_face(g, q, axis, (float)m.c1);
     }
     if (!g.face_in_bounds(q, axis)) {
       valid = false;
@@ -502,42 +532,99 @@ DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
              ? corrected
              : forward;
 }
-__global__ void __launch_bounds__(NT) k_mac(Dev D, int op) {
-  if (!setup_on(D)) return;
-  Motion m(D);
-  Mac mc(m);
-  long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  if (i >= D.NF) return;
+// One advecting face of op 27 (forward pass) or op 28 (corrected pass).
+template <int op, bool cached> DI void mac_face(const Dev& D, const Motion& m, const Mac& mc, long long i) {
   I3 q;
   int axis;
   m.g.unpack_face(i, q, axis);
   F3 x = face_x(D, m.g, q, axis);
-  float value = 0.f;
+  float value;
   float d = m.dt;
-  if (!m.g.wall_face(q, axis) && ((D.flags & 2) == 0 || mc.vb[i] > .5f)) {
-    if (D.flags & 4) {
-      if (op == 27) value = mac_forward(mc, x, axis, d, i, nullptr);
-      else value = mac_correct(mc, x, axis, d, i);
-    } else if (op == 27) {
-      bool valid;
-      float l0, l1v;
-      value = mc.sample(mc.trace(x, d), axis, false, valid, l0, l1v);
-    } else {
-      bool valid, vf;
-      float l0, l1v, d0, d1;
-      float backward = mc.sample(mc.trace(x, -d), axis, true, valid, l0, l1v);
-      mc.sample(mc.trace(x, d), axis, false, vf, d0, d1);
-      float forward = D.fwd[i], corrected = forward + .5f * (m.A[D.N + i] - backward);
-      value = (valid && vf && mc.trace_supported(x, d) && mc.trace_supported(x, -d) && corrected >= d0 && corrected <= d1)
-                  ? corrected
-                  : forward;
-    }
+  if constexpr (cached) {
+    if constexpr (op == 27) value = mac_forward(mc, x, axis, d, i, nullptr);
+    else value = mac_correct(mc, x, axis, d, i);
+  } else if constexpr (op == 27) {
+    bool valid;
+    float l0, l1v;
+    value = mc.sample(mc.trace(x, d), axis, false, valid, l0, l1v);
+  } else {
+    bool valid, vf;
+    float l0, l1v, d0, d1;
+    float backward = mc.sample(mc.trace(x, -d), axis, true, valid, l0, l1v);
+    mc.sample(mc.trace(x, d), axis, false, vf, d0, d1);
+    float forward = D.fwd[i], corrected = forward + .5f * (m.A[D.N + i] - backward);
+    value = (valid && vf && mc.trace_supported(x, d) && mc.trace_supported(x, -d) && corrected >= d0 && corrected <= d1)
+                ? corrected
+                : forward;
   }
-  if (op == 27) D.fwd[i] = value;
+  if constexpr (op == 27) D.fwd[i] = value;
   else m.Cb[D.N + i] = value;
 }
+
+// Work list of ops 27/28, rebuilt every trial.  The faces that advect (not wall faces; inside the
+// valid band when flag 2 is set) are listed, those within three cells (x, y) of a solid cell or of
+// the domain edge (the donor slow path) at the back of the list, the rest at the front; every
+// warp appends its faces contiguously.  A face that does not advect gets its op 27/28 results
+// (zero) here.  mac_ctr: [0] interior count, [1] boundary count, [2]/[3] op 27/28 work cursors.
+__global__ void k_mac_reset(const __grid_constant__ Dev D) {
+  if (threadIdx.x < 4) D.mac_ctr[threadIdx.x] = 0u;
+}
+__global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) {
+  if (!setup_on(D)) return;
+  Motion m(D);
+  const float* vb = m.acc == 0 ? D.vband0 : D.vband1;
+  const long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  bool act = false, edge = false;
+  if (i < D.NF) {
+    I3 q;
+    int axis;
+    m.g.unpack_face(i, q, axis);
+    act = !m.g.wall_face(q, axis) && ((D.flags & 2) == 0 || vb[i] > .5f);
+    if (act) edge = D.mac_class[(axis * (D.ny + 1) + q.y) * (D.nx + 1) + q.x] != 0;
+    else {
+      D.fwd[i] = 0.f;
+      m.Cb[D.N + i] = 0.f;
+    }
+  }
+  const unsigned be = __ballot_sync(0xffffffffu, act && edge), bi = __ballot_sync(0xffffffffu, act && !edge);
+  const int lane = threadIdx.x & 31;
+  unsigned base_e = 0, base_i = 0;
+  if (lane == 0) {
+    if (be) base_e = atomicAdd(&D.mac_ctr[1], (unsigned)__popc(be));
+    if (bi) base_i = atomicAdd(&D.mac_ctr[0], (unsigned)__popc(bi));
+  }
+  base_e = __shfl_sync(0xffffffffu, base_e, 0);
+  base_i = __shfl_sync(0xffffffffu, base_i, 0);
+  if (act) {
+    const unsigned below = (unsigned)__popc((edge ? be : bi) & ((1u << lane) - 1u));
+    if (edge) D.mac_list[D.NF - 1 - (long long)(base_e + below)] = (int)i;
+    else D.mac_list[base_i + below] = (int)i;
+  }
+}
+// Persistent pass over the work list: each warp takes 32 consecutive entries at a time, boundary
+// faces first, so a slow warp never holds idle lanes of a finished block.
+template <int op, bool cached> __global__ void __launch_bounds__(NT) k_mac(const __grid_constant__ Dev D) {
+  if (!setup_on(D)) return;
+  const unsigned n_int = D.mac_ctr[0], n_edge = D.mac_ctr[1], total = n_int + n_edge;
+  unsigned* cursor = D.mac_ctr + (op == 27 ? 2 : 3);
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    __syncwarp();
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(cursor, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const unsigned k = base + lane;
+    if (k < total) {
+      const long long i = k < n_edge ? (long long)D.mac_list[D.NF - 1 - (long long)k] : (long long)D.mac_list[k - n_edge];
+      Motion m(D);  // views of the parameter block, rebuilt per face so none of it stays live
+      Mac mc(m);
+      mac_face<op, cached>(D, m, mc, i);
+    }
+  }
+}
 // Debug probe: the op-27 forward trace of one face (16 floats + value).
-__global__ void k_debug_face(Dev D, long long i, float* out) {
+__global__ void k_debug_face(const __grid_constant__ Dev D, long long i, float* out) {
   Motion m(D);
   Mac mc(m);
   I3 q;
@@ -551,7 +638,7 @@ __global__ void k_debug_face(Dev D, long long i, float* out) {
 }
 
 // Debug probe: one sampled component with its eight donors (include/waves_debug.h).
-__global__ void k_debug_sample(Dev D, float x, float y, float z, int axis, int forward, float* out) {
+__global__ void k_debug_sample(const __grid_constant__ Dev D, float x, float y, float z, int axis, int forward, float* out) {
   Motion m(D);
   Mac mc(m);
   bool valid;
@@ -587,16 +674,37 @@ void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis,
 }
 
 void launch_motion_cfl(const Dev& D, cudaStream_t s) {
+  const unsigned wt = grid_for((long long)D.wt_w * D.wt_h);
+  if (D.coastal) k_wave_tables<<<wt, NT, 0, s>>>(D, 0);
   k_cfl<<<grid_for(D.N), NT, 0, s>>>(D);
+  if (D.coastal) k_wave_tables<<<wt, NT, 0, s>>>(D, 1);
   k_compress<<<grid_for(D.N), NT, 0, s>>>(D);
 }
 void launch_sweep(const Dev& D, cudaStream_t s) {
   k_sweep_plane<<<grid_for(D.N), NT, 0, s>>>(D);
-  k_sweep_update<<<grid_for(D.N), NT, 0, s>>>(D);
+  // reads F, the plane field (16 B), the sweep-axis faces and c_i; writes F
+  probed(kProbeSweepVof, s, 32.0 * (double)D.N, [&] { k_sweep_update<<<grid_for(D.N), NT, 0, s>>>(D); });
+}
+int mac_blocks() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mac<28, true>, NT, 0) != cudaSuccess)
+    return 0;
+  return sms * (per_sm > 0 ? per_sm : 1);
 }
 void launch_maccormack(const Dev& D, cudaStream_t s) {
-  k_mac<<<grid_for(D.NF), NT, 0, s>>>(D, 27);
-  k_mac<<<grid_for(D.NF), NT, 0, s>>>(D, 28);
+  k_mac_reset<<<1, 32, 0, s>>>(D);
+  k_mac_list<<<grid_for(D.NF), NT, 0, s>>>(D);
+  // op 27 reads the accepted faces and valid band, writes the forward values (and, with the trace
+  // cache, its six fields); op 28 reads those, the faces and the band, and writes the candidate.
+  const double nf = (double)D.NF, cache = (D.flags & 4) ? 6.0 : 0.0;
+  if (D.flags & 4) {
+    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { k_mac<27, true><<<D.mac_grid, NT, 0, s>>>(D); });
+    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { k_mac<28, true><<<D.mac_grid, NT, 0, s>>>(D); });
+  } else {
+    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { k_mac<27, false><<<D.mac_grid, NT, 0, s>>>(D); });
+    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { k_mac<28, false><<<D.mac_grid, NT, 0, s>>>(D); });
+  }
 }
 
 }  // namespace wg

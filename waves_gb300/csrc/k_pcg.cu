@@ -35,7 +35,7 @@ DI float operator_at(const Dev& D, const Grid& g, I3 q, long long i, const float
 namespace {
 
 // ---------------------------------------------------------------- op 3 (+ op 4 when the V-cycle is off)
-__global__ void __launch_bounds__(NT) k_cg_init(Dev D) {
+__global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
   if (!pressure_setup(D)) return;
   Grid g(D);
   const float* Cb = bank_ptr(D, 1 - acc_bank(D));
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 5 + 6 + 7
-__global__ void __launch_bounds__(NT) k_cg_matvec(Dev D) {
+__global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D) {
   if (!solving(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 8 + multigrid load (op 5 of the cycle)
-template <class T> __global__ void __launch_bounds__(NT) k_cg_update(Dev D) {
+template <class T> __global__ void __launch_bounds__(NT) k_cg_update(const __grid_constant__ Dev D) {
   if (!solving(D)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -120,7 +120,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_cg_update(Dev D) {
 }
 
 // ---------------------------------------------------------------- op 10 (+ loop condition)
-__global__ void __launch_bounds__(NT) k_cg_direction(Dev D, cudaGraphConditionalHandle h, int use_handle) {
+__global__ void __launch_bounds__(NT) k_cg_direction(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int use_handle) {
   bool on = solving(D);
   if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) {
     // The body has run ops 5-10 of one iteration; continue while solving.
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(NT) k_cg_direction(Dev D, cudaGraphConditional
 }
 
 // ---------------------------------------------------------------- graph conditions
-__global__ void k_set_cond(Dev D, cudaGraphConditionalHandle h, int which) {
+__global__ void k_set_cond(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int which) {
   const double* c = D.c;
   bool v;
   if (which == kCondDefectFirst) v = true;
@@ -145,7 +145,7 @@ __global__ void k_set_cond(Dev D, cudaGraphConditionalHandle h, int which) {
 }
 
 // ---------------------------------------------------------------- ops 43 + 1 (trial begin) and 63/64
-__global__ void k_begin(Dev D) {
+__global__ void k_begin(const __grid_constant__ Dev D) {
   double* c = D.c;
   // op 43 (coupled_motion.glslinc:351-355)
   bool retry = c[7] == 20 || (c[7] >= 10 && c[7] <= 12);
@@ -161,7 +161,7 @@ __global__ void k_begin(Dev D) {
     c[32] += 1; c[57] = 0; c[58] = 0;
   }
 }
-__global__ void __launch_bounds__(NT) k_defect_begin(Dev D) {
+__global__ void __launch_bounds__(NT) k_defect_begin(const __grid_constant__ Dev D) {
   const double* c = D.c;
   double c57 = c[57];
   bool go = (c57 == 1 || c57 == 2) && c[7] < .5;

@@ -2,11 +2,46 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "dev.h"
 
 namespace wg {
 
 enum CondKind { kCondActive = 0, kCondSolving = 1, kCondDefect = 2, kCondDefectFirst = 3 };
+
+// Kernel probes.  While a probe list is installed on the calling thread (host-scheduled trials
+// only, never during graph capture), each probed launch site brackets its launch with two events
+// on its stream and records the launch's algorithmic bytes: the distinct input arrays read once
+// and the outputs written once, at storage precision.
+enum ProbeKind {
+  kProbeMac = 0,        // k_mac, MacCormack forward (op 27) and corrected (op 28) passes
+  kProbeSmooth0 = 1,    // k_mg0_cheb, level-0 Chebyshev sweeps
+  kProbeRows = 2,       // k_mgl_rows, level >= 1 sweeps with the product-parallel apply
+  kProbeRowThread = 3,  // k_mgl ops 0-2, level >= 1 sweeps with one thread per row
+  kProbeSweepVof = 4,   // k_sweep_update, VOF flux + update of one direction
+  kProbeCount = 5
+};
+struct ProbeRec {
+  int kind;
+  cudaEvent_t a, b;
+  double bytes;
+};
+extern thread_local std::vector<ProbeRec>* g_probe;
+template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launch) {
+  std::vector<ProbeRec>* p = g_probe;
+  if (!p) {
+    launch();
+    return;
+  }
+  ProbeRec r{kind, nullptr, nullptr, bytes};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, s);
+  launch();
+  cudaEventRecord(r.b, s);
+  p->push_back(r);
+}
 
 // k_pcg.cu
 void launch_begin(const Dev& D, cudaStream_t s);
@@ -20,6 +55,7 @@ void launch_set_cond(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h,
 void launch_motion_cfl(const Dev& D, cudaStream_t s);
 void launch_sweep(const Dev& D, cudaStream_t s);
 void launch_maccormack(const Dev& D, cudaStream_t s);
+int mac_blocks();  // resident blocks of the persistent MacCormack kernel on the current device
 void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis, int forward, float* out);
 // k_geom.cu
 void launch_coastal(const Dev& D, cudaStream_t s);

@@ -20,10 +20,15 @@
 #include <vector>
 
 #include "../../include/waves.h"
+#include "../../include/waves_debug.h"
 #include "dev.h"
 #include "kernels.h"
 
 using wg::Dev;
+
+namespace wg {
+thread_local std::vector<ProbeRec>* g_probe = nullptr;
+}
 
 namespace {
 
@@ -284,7 +289,10 @@ waves_status setup_device(waves_handle* h) {
   AL(D.history, 4 * (size_t)cap, true, "history");
   AL(D.chistory, 5 * (size_t)cap, true, "chistory");
   AL(D.c, WAVES_CONTROL_SIZE, true, "control");
-  long long maxblocks = (std::max(std::max(N, NF), S) + 255) / 256 + 1;
+  // every grid that writes reduction partials: one block per 256 entries, or the level-0 tiles
+  // of 32 x 8 cells per z plane
+  long long tiles0 = (long long)((D.nx + 31) / 32) * ((D.ny + 7) / 8) * D.nz;
+  long long maxblocks = std::max((std::max(std::max(N, NF), S) + 255) / 256 + 1, tiles0);
   AL(D.part, 9 * maxblocks, false, "partials");
   AL(D.count, wg::kSiteCount, false, "counters");
   AL(h->probes, 8, true, "probes");
@@ -311,8 +319,42 @@ waves_status setup_device(waves_handle* h) {
     AL(dclear, clear.size(), false, "clear_table");
     CK(cudaMemcpyAsync(dclear, clear.data(), clear.size(), cudaMemcpyHostToDevice, h->stream));
     D.clear_tab = dclear;
+    // MacCormack face class per (axis, y, x) column: 1 within three cells of a solid cell or of the
+    // domain edge (where donors take the boundary path), every column when x is periodic.
+    const int cx = D.nx + 1, cy = D.ny + 1;
+    std::vector<unsigned char> cls((size_t)3 * cx * cy, 1);
+    if (!D.px)
+      for (int y = 0; y < cy; y++)
+        for (int x = 0; x < cx; x++) {
+          bool edge = x < 3 || x > D.nx - 4 || y < 3 || y > D.ny - 4;
+          for (int dy = -3; dy <= 3 && !edge; dy++)
+            for (int dx = -3; dx <= 3 && !edge; dx++) edge = solid_host(k, x + dx, y + dy);
+          for (int a = 0; a < 3; a++) cls[((size_t)a * cy + y) * cx + x] = edge ? 1 : 0;
+        }
+    unsigned char* dcls;
+    AL(dcls, cls.size(), false, "mac_class");
+    CK(cudaMemcpyAsync(dcls, cls.data(), cls.size(), cudaMemcpyHostToDevice, h->stream));
+    D.mac_class = dcls;
     CK(cudaStreamSynchronize(h->stream));
   }
+  // wave-target tables: columns from 4 ghost columns left of x = 0 to the last face column of the
+  // forcing zone, rows 0..ny; the stamps start as NaN, which no time equals
+  D.wt_x0 = -4;
+  D.wt_w = D.coastal ? D.zone_x_end + 2 - D.wt_x0 : 0;
+  D.wt_h = D.coastal ? D.ny + 1 : 0;
+  if (D.coastal) {
+    AL(D.wsurf, (size_t)3 * D.wt_w, false, "wave_surface");
+    AL(D.wvel, (size_t)6 * D.wt_h * D.wt_w, false, "wave_velocity");
+    AL(D.wdecay, (size_t)2 * D.wt_w, false, "wave_relaxation");
+    AL(D.wstamp, 4, false, "wave_stamps");
+    const float nan4[4] = {NAN, NAN, NAN, NAN};
+    CK(cudaMemcpyAsync(D.wstamp, nan4, sizeof(nan4), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  AL(D.mac_list, NF, false, "mac_list");
+  AL(D.mac_ctr, 4, false, "mac_counters");
+  D.mac_grid = wg::mac_blocks();
+  if (D.mac_grid <= 0) D.mac_grid = 2 * 152;
   // multigrid
   plan_levels(h);
   if ((int)h->levels.size() > wg::kMaxLevels) {
@@ -442,6 +484,9 @@ waves_status setup_device(waves_handle* h) {
     int v = atoi(e);
     if (v >= 1 && v < D.L) D.mg_bottom = v;
   }
+  // Levels with fewer rows than this use the product-parallel apply (both forms give the same bits).
+  D.mg_rows_below = 65536;
+  if (const char* e = getenv("WAVES_MG_ROWS_BELOW")) D.mg_rows_below = std::max(0, atoi(e));
   AL(D.mgmat, moff, true, "mg_matrix");
   {
     void* p;
@@ -653,8 +698,9 @@ waves_status upload_quota(waves_handle* h) {
   return WAVES_OK;
 }
 
-// Host-driven trial: same kernels, control flow decided from the control block.
-waves_status host_trial(waves_handle* h) {
+// Host-driven trial: same kernels, control flow decided from the control block, read after every
+// `batch` CG iterations (iterations past convergence return at once).
+waves_status host_trial(waves_handle* h, int batch = 4) {
   const Dev& D = h->D;
   cudaStream_t s = h->stream;
   wg::launch_begin(D, s);
@@ -667,7 +713,7 @@ waves_status host_trial(waves_handle* h) {
     if ((st = read_control(h)) != WAVES_OK) return st;
     const double* c = h->host_c;
     while (c[4] > .5 && c[6] < .5 && c[7] < .5) {
-      for (int k = 0; k < 4; k++) enqueue_cg_iteration(h, s, 0, 0);
+      for (int k = 0; k < batch; k++) enqueue_cg_iteration(h, s, 0, 0);
       if ((st = read_control(h)) != WAVES_OK) return st;
     }
     wg::launch_post(D, s);
@@ -1089,6 +1135,34 @@ waves_status waves_debug_sample(waves_handle* h, const float* x, int32_t axis, i
   cudaFree(d);
   return WAVES_OK;
 }
+waves_status waves_debug_probe_trial(waves_handle* h, waves_kernel_probe* out, int32_t capacity, int32_t* trials) {
+  if (!h || !out || capacity < 1) return WAVES_INVALID_ARG;
+  if (h->cfg.iterations_per_batch < 1) return WAVES_INVALID_ARG;
+  for (int k = 0; k < capacity; k++) out[k] = waves_kernel_probe{k, 0, 0.0, 0.0};
+  std::vector<wg::ProbeRec> recs;
+  wg::g_probe = &recs;
+  waves_status st = WAVES_OK;
+  int32_t done = 0;
+  // one host-scheduled trial with every CG iteration checked: no probed launch is a no-op
+  if ((st = upload_quota(h)) == WAVES_OK) st = host_trial(h, 1);
+  wg::g_probe = nullptr;
+  if (st == WAVES_OK) done = 1;
+  if (st == WAVES_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) st = WAVES_CUDA_ERROR;
+  for (const wg::ProbeRec& r : recs) {
+    float ms = 0.f;
+    if (st == WAVES_OK && r.kind < capacity && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      out[r.kind].launches++;
+      out[r.kind].ms += ms;
+      out[r.kind].bytes += r.bytes;
+    }
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  if (trials) *trials = done;
+  cudaGetLastError();
+  return st;
+}
+
 waves_status waves_debug_launch_counts(waves_handle* h, int32_t* out8) {
   if (!h || !out8) return WAVES_INVALID_ARG;
   std::memcpy(out8, h->launches, sizeof(h->launches));
