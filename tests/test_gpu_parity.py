@@ -72,11 +72,13 @@ def test_step_parity(gpu_lib, name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["beach_slope", "beach_slope_bf16"])
-def test_step_parity_row_per_thread(gpu_lib, name, monkeypatch):
-    """The multigrid levels >= 1 have two apply kernels (product-parallel rows for small levels,
-    one thread per row for large ones); the small grids above use only the first, so force the
-    second on every level here."""
-    monkeypatch.setenv("WAVES_MG_ROWS_BELOW", "0")
+@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1"])
+def test_step_parity_kernel_variants(gpu_lib, name, variant, monkeypatch):
+    """Kernel forms that the small grids above do not reach: the level >= 1 sweeps with one
+    thread per row (large levels use it; small ones use the product-parallel rows), and the
+    bottom levels solved from global memory (used when they do not fit the shared-memory stage)."""
+    key, value = variant.split("=")
+    monkeypatch.setenv(key, value)
     cfg = CASES[name]()
     g = wg.WavesSolver(cfg)
     o = Oracle(cfg, 32)

@@ -49,6 +49,14 @@ DI float mxf(float a, float b) { return (a < b) ? b : a; }
 DI float clampf_(float x, float lo, float hi) { return mnf(mxf(x, lo), hi); }
 DI float fract_(float x) { return x - floorf(x); }
 DI float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+// griddepcontrol.wait: returns once the grid this one depends on (programmatic launch) has
+// completed and its memory is visible (immediate for a normally launched kernel); then
+// griddepcontrol.launch_dependents lets the next kernel on the stream be scheduled once every
+// block of this grid is resident (it still waits for this grid to complete before it reads).
+DI void grid_dep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 DI float tcos(float x) { return (float)cos((double)x); }
 DI float tsin(float x) { return (float)sin((double)x); }
 DI float ttanh(float x) { return (float)tanh((double)x); }
@@ -70,7 +78,11 @@ struct Grid {
   DI explicit Grid(const Dev& d) : D(d) {}
   DI float h(int a) const { return a == 0 ? D.hx : (a == 1 ? D.hy : D.hz); }
   DI long long index3(I3 q) const { return (long long)q.x + (long long)D.nx * ((long long)q.y + (long long)D.ny * q.z); }
-  DI I3 coord(long long i) const { return mk(int(i % D.nx), int((i / D.nx) % D.ny), int(i / ((long long)D.nx * D.ny))); }
+  // cell and face counts stay below 2^31, so the index arithmetic runs in 32-bit unsigned integers
+  DI I3 coord(long long i) const {
+    const unsigned u = (unsigned)i, nx = (unsigned)D.nx, row = u / nx;
+    return mk(int(u - row * nx), int(row % (unsigned)D.ny), int(row / (unsigned)D.ny));
+  }
   DI I3 wrap_cell(I3 q) const {
     q.z = pidx(q.z, D.nz);
     if (D.px) q.x = pidx(q.x, D.nx);
@@ -138,8 +150,8 @@ struct Grid {
     if (f < D.NU) { axis = 0; base = 0; mx_ = D.nx + 1; my_ = D.ny; }
     else if (f < D.NU + D.NV) { axis = 1; base = D.NU; mx_ = D.nx; my_ = D.ny + 1; }
     else { axis = 2; base = D.NU + D.NV; mx_ = D.nx; my_ = D.ny; }
-    long long i = f - base;
-    q = mk(int(i % mx_), int((i / mx_) % my_), int(i / ((long long)mx_ * my_)));
+    const unsigned u = (unsigned)(f - base), row = u / (unsigned)mx_;
+    q = mk(int(u - row * (unsigned)mx_), int(row % (unsigned)my_), int(row / (unsigned)my_));
   }
   DI bool wall_face(I3 q, int axis) const { return solid(q) || solid(ax(q, axis, -1)); }
   DI bool face_in_bounds(I3 q, int axis) const {

@@ -8,6 +8,7 @@ namespace wg {
 
 constexpr int kMaxLevels = 12;
 constexpr int kMaxStencil = 125;
+constexpr int kBottomSmemMax = 200 * 1024;  // shared-memory stage of the bottom levels
 constexpr int kSolidPad = 16;  // margin of the tabulated solid() lookup
 
 // Indices into the double control block beyond the reference's 96 entries.
@@ -135,6 +136,7 @@ struct Dev {
   int* mgcol;                // ELL columns of levels >= 1, same layout as mgell
   int mg_bottom;             // first level solved by the single-block bottom kernel
   int mg_rows_below;         // levels with fewer rows use the product-parallel apply
+  int mg_bottom_smem;        // bytes of the shared-memory bottom stage (0: bottom levels too large)
 };
 
 // Reduction sites (one last-block counter each).

@@ -224,6 +224,7 @@ DI bool post_on(const Dev& D) { return D.c[4] > .5 && D.c[6] > .5 && D.c[7] < .5
 
 // ---------------------------------------------------------------- op 17 (+ coastal op 87/88)
 __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D, int op, int with_bounds) {
+  grid_dep_wait();
   bool on = op == 19 ? !(D.c[4] > .5) : geometry_on(D);
   bool bounds = with_bounds && setup_on(D);
   if (!on && !bounds) return;
@@ -253,6 +254,7 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- op 18
 __global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!geometry_on(D)) return;
   Geo G(D, 18);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -265,6 +267,7 @@ __global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) 
 
 // ---------------------------------------------------------------- op 16
 __global__ void __launch_bounds__(NT) k_geom_coef(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!geometry_on(D)) return;
   Geo G(D, 16);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -285,6 +288,7 @@ __global__ void __launch_bounds__(NT) k_geom_coef(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- op 2 + op 47
 __global__ void __launch_bounds__(NT) k_proj_setup(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!(D.c[5] > .5)) return;
   Geo G(D, 2);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -313,6 +317,7 @@ __global__ void __launch_bounds__(NT) k_proj_setup(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- op 11 (gradient apply)
 __global__ void __launch_bounds__(NT) k_grad_apply(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!post_on(D)) return;
   Geo G(D, 11);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -332,6 +337,7 @@ __global__ void __launch_bounds__(NT) k_grad_apply(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- ops 30-33 (nearest sources)
 __global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -343,6 +349,7 @@ __global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) 
   D.src0[f] = (!g.wall_face(q, axis) && (g.wet(q) || g.wet(l))) ? pack_face(q) : -1;
 }
 __global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, int rb) {
+  grid_dep_wait();
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -403,6 +410,7 @@ DI float extended_value(const Dev& D, const Grid& g, const float* Cb, int packed
 
 // ---------------------------------------------------------------- op 34 + 47 + 48
 __global__ void __launch_bounds__(NT) k_ext_write(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!post_on(D)) return;
   Grid g(D);
   int cand = 1 - acc_bank(D);
@@ -434,6 +442,7 @@ __global__ void __launch_bounds__(NT) k_ext_write(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- ops 35/36, 62/66, 65, 12/13
 __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!post_on(D)) return;
   Geo G(D, 12);
   const Grid& g = G.g;
@@ -523,6 +532,7 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- ops 44, 85, 89 (one block)
 __global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   __shared__ float cols[8 * 128];
   Grid g(D);
   const float* A = bank_ptr(D, acc_bank(D));
@@ -572,6 +582,7 @@ __global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- coastal ops 80-84
 __global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Geo G(D, 80);
   const Grid& g = G.g;
@@ -579,9 +590,8 @@ __global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev 
   long long t = (long long)blockIdx.x * NT + threadIdx.x;
   double v[4] = {0, 0, 0, 0};
   if (t < cells) {
-    int x = (int)(t % D.zone_x_end);
-    long long rest = t / D.zone_x_end;
-    I3 q = mk(x, (int)(rest % D.ny), (int)(rest / D.ny));
+    const unsigned zx = (unsigned)D.zone_x_end, rest = (unsigned)t / zx;
+    I3 q = mk(int((unsigned)t - rest * zx), int(rest % (unsigned)D.ny), int(rest / (unsigned)D.ny));
     if (!g.solid(q)) {
       long long i = g.index3(q);
       float time = (float)(D.c[1] + D.c[20]);
@@ -612,6 +622,7 @@ __global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev 
   }
 }
 __global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Geo G(D, 82);
   const Grid& g = G.g;
@@ -626,7 +637,8 @@ __global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev 
   if (t < nu) { axis = 0; rest = t; my_ = D.ny; }
   else if (t < nu + nv) { axis = 1; rest = t - nu; my_ = D.ny + 1; }
   else { axis = 2; rest = t - nu - nv; my_ = D.ny; }
-  I3 q = mk((int)(rest % zx), (int)((rest / zx) % my_), (int)(rest / ((long long)zx * my_)));
+  const unsigned ur = (unsigned)rest, row = ur / (unsigned)zx;
+  I3 q = mk(int(ur - row * (unsigned)zx), int(row % (unsigned)my_), int(row / (unsigned)my_));
   int mxl = D.nx + (axis == 0);
   if (q.x >= mxl) return;
   long long f;
@@ -646,6 +658,7 @@ __global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev 
   D.fwd[f] = value - old;
 }
 __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Geo G(D, 83);
   const Grid& g = G.g;
@@ -653,9 +666,8 @@ __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ D
   long long t = (long long)blockIdx.x * NT + threadIdx.x;
   double v[3] = {0, 0, 0};
   if (t < cells) {
-    int x = (int)(t % D.zone_x_end);
-    long long rest = t / D.zone_x_end;
-    I3 q = mk(x, (int)(rest % D.ny), (int)(rest / D.ny));
+    const unsigned zx = (unsigned)D.zone_x_end, rest = (unsigned)t / zx;
+    I3 q = mk(int((unsigned)t - rest * zx), int(rest % (unsigned)D.ny), int(rest / (unsigned)D.ny));
     long long i = g.index3(q);
     float m = G.Cb[i] * 1000.f;
     for (int axis = 0; axis < 3; axis++) {
@@ -673,6 +685,7 @@ __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ D
 
 // ---------------------------------------------------------------- export (op 19) into buffers
 __global__ void __launch_bounds__(NT) k_export(const __grid_constant__ Dev D, float4* planes, float* kinds) {
+  grid_dep_wait();
   Geo G(D, 19);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -689,28 +702,28 @@ void launch_coastal(const Dev& D, cudaStream_t s) {
   long long cells = (long long)D.zone_x_end * D.ny * D.nz;
   int zx = D.zone_x_end + 1;
   long long faces = (long long)zx * D.ny * D.nz + (long long)zx * (D.ny + 1) * D.nz + (long long)zx * D.ny * (D.nz + 1);
-  k_coast_cells<<<grid_for(cells), NT, 0, s>>>(D);
-  k_coast_faces<<<grid_for(faces), NT, 0, s>>>(D);
-  k_coast_momentum<<<grid_for(cells), NT, 0, s>>>(D);
+  pdl_launch(k_coast_cells, grid_for(cells), NT, 0, s, D);
+  pdl_launch(k_coast_faces, grid_for(faces), NT, 0, s, D);
+  pdl_launch(k_coast_momentum, grid_for(cells), NT, 0, s, D);
 }
 void launch_geometry(const Dev& D, cudaStream_t s) {
-  k_geom_plane<<<grid_for(D.N), NT, 0, s>>>(D, 17, D.coastal);
-  k_geom_phi<<<grid_for(D.N), NT, 0, s>>>(D);
-  k_geom_coef<<<grid_for(D.N), NT, 0, s>>>(D);
+  pdl_launch(k_geom_plane, grid_for(D.N), NT, 0, s, D, 17, D.coastal);
+  pdl_launch(k_geom_phi, grid_for(D.N), NT, 0, s, D);
+  pdl_launch(k_geom_coef, grid_for(D.N), NT, 0, s, D);
 }
-void launch_proj_setup(const Dev& D, cudaStream_t s) { k_proj_setup<<<grid_for(D.S), NT, 0, s>>>(D); }
+void launch_proj_setup(const Dev& D, cudaStream_t s) { pdl_launch(k_proj_setup, grid_for(D.S), NT, 0, s, D); }
 void launch_post(const Dev& D, cudaStream_t s) {
-  k_grad_apply<<<grid_for(D.NF), NT, 0, s>>>(D);
-  k_ext_init<<<grid_for(D.NF), NT, 0, s>>>(D);
-  k_ext_step<<<grid_for(D.NF), NT, 0, s>>>(D, 0);
-  k_ext_step<<<grid_for(D.NF), NT, 0, s>>>(D, 1);
-  k_ext_step<<<grid_for(D.NF), NT, 0, s>>>(D, 0);
-  k_ext_write<<<grid_for(D.NF > D.N ? D.NF : D.N), NT, 0, s>>>(D);
-  k_accept<<<grid_for(D.N), NT, 0, s>>>(D);
+  pdl_launch(k_grad_apply, grid_for(D.NF), NT, 0, s, D);
+  pdl_launch(k_ext_init, grid_for(D.NF), NT, 0, s, D);
+  pdl_launch(k_ext_step, grid_for(D.NF), NT, 0, s, D, 0);
+  pdl_launch(k_ext_step, grid_for(D.NF), NT, 0, s, D, 1);
+  pdl_launch(k_ext_step, grid_for(D.NF), NT, 0, s, D, 0);
+  pdl_launch(k_ext_write, grid_for(D.NF > D.N ? D.NF : D.N), NT, 0, s, D);
+  pdl_launch(k_accept, grid_for(D.N), NT, 0, s, D);
 }
-void launch_trial_end(const Dev& D, cudaStream_t s) { k_trial_end<<<1, NT, 0, s>>>(D); }
+void launch_trial_end(const Dev& D, cudaStream_t s) { pdl_launch(k_trial_end, 1, NT, 0, s, D); }
 void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds) {
-  k_export<<<grid_for(D.N), NT, 0, s>>>(D, planes, kinds);
+  pdl_launch(k_export, grid_for(D.N), NT, 0, s, D, planes, kinds);
 }
 
 }  // namespace wg

@@ -10,6 +10,7 @@ constexpr int NT = 256;
 
 // op 0 (pressure_pass.glslinc:182-198)
 __global__ void __launch_bounds__(NT) k_init_still(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.S) return;
@@ -43,6 +44,7 @@ DI float block_overlap(const Dev& D, F3 lo, F3 hi, F3 lower, F3 upper) {
 }
 // op 40 (coupled_motion.glslinc:234-270)
 __global__ void __launch_bounds__(NT) k_init_fixture(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   int shape = D.shape;
@@ -96,6 +98,7 @@ __global__ void __launch_bounds__(NT) k_init_fixture(const __grid_constant__ Dev
 
 // op 41/42
 __global__ void __launch_bounds__(NT) k_init_volume(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   double v[1] = {0};
   if (i < D.N) v[0] = (double)bank_ptr(D, acc_bank(D))[i] * D.cell_d;
@@ -106,6 +109,7 @@ __global__ void __launch_bounds__(NT) k_init_volume(const __grid_constant__ Dev 
 
 // op 49 (coupled_motion.glslinc:323-337)
 __global__ void __launch_bounds__(NT) k_init_masks(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i < D.N) {
@@ -126,6 +130,7 @@ __global__ void __launch_bounds__(NT) k_init_masks(const __grid_constant__ Dev D
 
 // op 86 (coastal_pass.glslinc:78-83)
 __global__ void k_probes(const __grid_constant__ Dev D, float4* out) {
+  grid_dep_wait();
   int i = threadIdx.x;
   if (i >= 8) return;
   Coast cs(D);
@@ -141,15 +146,15 @@ unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
 }  // namespace
 
 void launch_initial(const Dev& D, cudaStream_t s, float4* probes) {
-  k_init_still<<<grid_for(D.S), NT, 0, s>>>(D);
+  pdl_launch(k_init_still, grid_for(D.S), NT, 0, s, D);
   long long n = D.N > D.NF ? D.N : D.NF;
-  k_init_fixture<<<grid_for(n), NT, 0, s>>>(D);
+  pdl_launch(k_init_fixture, grid_for(n), NT, 0, s, D);
   launch_geometry(D, s);
-  k_init_volume<<<grid_for(D.N), NT, 0, s>>>(D);
-  k_init_masks<<<grid_for(n), NT, 0, s>>>(D);
+  pdl_launch(k_init_volume, grid_for(D.N), NT, 0, s, D);
+  pdl_launch(k_init_masks, grid_for(n), NT, 0, s, D);
   if (D.coastal) {
     launch_trial_end(D, s);  // op 85 (ops 44 and 89 are inert before the first trial)
-    k_probes<<<1, 32, 0, s>>>(D, probes);
+    pdl_launch(k_probes, 1, 32, 0, s, D, probes);
   }
 }
 

@@ -40,7 +40,8 @@ struct MG {
   }
   DI I3 coord(int l, int i) const {
     const MGLevelDev& v = D.lv[l];
-    return mk(i % v.nx, (i / v.nx) % v.ny, i / (v.nx * v.ny));
+    const unsigned u = (unsigned)i, row = u / (unsigned)v.nx;
+    return mk(int(u - row * (unsigned)v.nx), int(row % (unsigned)v.ny), int(row / (unsigned)v.ny));
   }
   DI I3 delta(int l, int i, int j) const {
     const MGLevelDev& v = D.lv[l];
@@ -190,6 +191,7 @@ DI unsigned signature(const Dev& D, const Grid& g, long long i) {
   return result;
 }
 __global__ void k_hs_reset(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   for (int k = 1; k <= 7; k++) s[k] = 0;
@@ -201,6 +203,7 @@ __global__ void k_hs_reset(const __grid_constant__ Dev D) {
 struct AddU { DI unsigned operator()(unsigned a, unsigned b) const { return a + b; } };
 struct MaxU { DI unsigned operator()(unsigned a, unsigned b) const { return a < b ? b : a; } };
 __global__ void __launch_bounds__(NT) k_hs_count(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D)) return;
   __shared__ unsigned sh[32];
   Grid g(D);
@@ -245,6 +248,7 @@ __global__ void __launch_bounds__(NT) k_hs_count(const __grid_constant__ Dev D) 
   }
 }
 __global__ void k_hs_decide(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   double* c = D.c;
@@ -268,6 +272,7 @@ __global__ void k_hs_decide(const __grid_constant__ Dev D) {
   }
 }
 template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -291,6 +296,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(const __g
   }
 }
 __global__ void k_hs_record(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   if (s[13] <= (unsigned)D.hist_cap) {
@@ -301,6 +307,7 @@ __global__ void k_hs_record(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- build ops
 template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[9] == 0) return;
   __shared__ unsigned sh[32];
   MG m(D);
@@ -327,6 +334,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_
   if (threadIdx.x == 0 && r) atomicAdd(&D.hstate[20 + l], r);
 }
 template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   if (!build_on(D) || !(D.hstate[14] == 0 || D.hstate[20 + l + 1] != 0)) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -342,6 +350,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __g
 }
 // l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -380,6 +389,7 @@ DI void child_range(const Dev& D, int l, int axis, int qc, int& lo, int& ext) {
 }
 // Deterministic Galerkin product of level l into level l+1 (replaces ops 2 + 3).
 template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __grid_constant__ Dev D, int l, int ex, int ey, int ez) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[8] == 0) return;
   extern __shared__ float part[];  // [125][GT]
   MG m(D);
@@ -440,6 +450,7 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
 }
 // ELL rows (pressure_multigrid.glslinc:176-182)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -456,6 +467,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_c
 }
 // Dense Cholesky and L^-1 of the last level (pressure_mg_coarse.glslinc:34-48), one block.
 template <class T> __global__ void k_mg_chol(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[8] == 0) return;
   __shared__ float dense[64 * 64];
   __shared__ float inv[64 * 64];
@@ -694,6 +706,7 @@ template <class T> DI float apply0(const Dev& D, const T* __restrict__ x, const 
 template <class T>
 __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, int phase, int source, float c1, float c2,
                                                   int first_k, int src_zero, int fin) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   const Cell0 c = cell0(D);
   double v[4] = {0, 0, 0, 0};
@@ -729,6 +742,7 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
   }
 }
 template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __grid_constant__ Dev D, int phase, int f) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   const Cell0 c = cell0(D);
   if (!c.ok) return;
@@ -736,6 +750,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __
 }
 // phase 0 load (op 5 of the cycle) fused with the first Chebyshev sweep from zero
 template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid_constant__ Dev D, int phase, int first_sweep) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -755,6 +770,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
 
 // Generic levels (l >= 1): one thread per cell.
 template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   __shared__ int lin[kMaxStencil];
   const int* lin_s = nullptr;
@@ -778,6 +794,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_cons
 // Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a level >= 1 with the
 // product-parallel apply: RR rows per block.
 template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   __shared__ float prod[kMaxStencil * RR];
   __shared__ bool inner[RR];
@@ -797,12 +814,37 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid
   }
 }
 
-// Whole sub-cycle from level lb down to the coarsest and back, in one block.
-// Returns (in *out_field) the field holding the level-lb correction.
-template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __grid_constant__ Dev D, int phase, int lb) {
-  if (!phase_on(D, phase)) return;
-  __shared__ float small[64];
-  MG m(D);
+// Shared-memory view of the bottom levels lb..L-1: their eight vector fields (one span per field,
+// levels in global order) and their ELL row values are staged in shared memory; columns are
+// recomputed from the stencil offsets (max(wrap(q + offset), 0), the cached columns), so apply()
+// reads the same values in the same order as the global-memory form.
+struct MGs : MG {
+  void* vec;
+  const void* ell;
+  int base_off, span;
+  long long base_eoff;
+  DI MGs(const Dev& d, void* v, const void* e, int lb, int sp)
+      : MG(d), vec(v), ell(e), base_off(d.lv[lb].off), span(sp), base_eoff(d.lv[lb].eoff) {}
+  template <class T> DI T* field(int f, int l) const { return (T*)vec + f * span + (D.lv[l].off - base_off); }
+  template <class T> DI bool active(int l, int i) const { return i >= 0 && ld_val(field<T>(3, l)[i]) > .5f; }
+  template <class T> DI float apply(int l, int f, int i, const int* = nullptr) const {
+    const T* x = field<T>(f, l);
+    if (!active<T>(l, i)) return ld_val(x[i]);
+    const MGLevelDev& lv = D.lv[l];
+    const T* e = (const T*)ell + (lv.eoff - base_eoff);
+    const I3 q = coord(l, i);
+    float sum = 0.f;
+    for (int k = 0; k < lv.stencil; k++) {
+      const int j = wrap(l, addI(q, offset(l, k)));
+      sum += ld_val(e[k * lv.count + i]) * ld_val(x[j > 0 ? j : 0]);
+    }
+    return sum;
+  }
+};
+
+// Whole sub-cycle from level lb down to the coarsest and back, in one block, over the view `m`
+// (global memory, or the shared-memory stage).  The level-lb correction ends in field 1.
+template <class T, class M> DI void bottom_cycle(const Dev& D, const M& m, int lb, float* small) {
   const int L = D.L;
   int field[kMaxLevels];
   auto each = [&](int l, auto fn) {
@@ -843,9 +885,39 @@ template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __g
     cf = smooth(l, f, false);
   }
 }
+template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __grid_constant__ Dev D, int phase, int lb) {
+  grid_dep_wait();
+  if (!phase_on(D, phase)) return;
+  __shared__ float small[64];
+  bottom_cycle<T>(D, MG(D), lb, small);
+}
+// The same with levels lb..L-1 staged in shared memory (D.mg_bottom_smem bytes: 8 fields of
+// `span` values, then the ELL values, 16-byte aligned): load, cycle, write the fields back.
+template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom_smem(const __grid_constant__ Dev D, int phase, int lb) {
+  grid_dep_wait();
+  if (!phase_on(D, phase)) return;
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ float small[64];
+  const int L = D.L;
+  const int span = D.lv[L - 1].off + D.lv[L - 1].count - D.lv[lb].off;
+  const long long e0 = D.lv[lb].eoff, e1 = D.lv[L - 1].eoff + (long long)D.lv[L - 1].stencil * D.lv[L - 1].count;
+  T* vec = (T*)stage;
+  T* ell = (T*)(stage + (((size_t)8 * span * sizeof(T) + 15) & ~(size_t)15));
+  const T* gvec = (const T*)D.mgv + D.lv[lb].off;
+  for (int f = 0; f < 8; f++)
+    for (int k = threadIdx.x; k < span; k += blockDim.x) vec[f * span + k] = gvec[(size_t)f * D.mg_nodes + k];
+  const T* gell = (const T*)D.mgell + e0;
+  for (long long k = threadIdx.x; k < e1 - e0; k += blockDim.x) ell[k] = gell[k];
+  __syncthreads();
+  bottom_cycle<T>(D, MGs(D, vec, ell, lb, span), lb, small);
+  T* out = (T*)D.mgv + D.lv[lb].off;
+  for (int f = 0; f < 8; f++)
+    for (int k = threadIdx.x; k < span; k += blockDim.x) out[(size_t)f * D.mg_nodes + k] = vec[f * span + k];
+}
 
 // op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __grid_constant__ Dev D, int phase, int f) {
+  grid_dep_wait();
   if (!phase_on(D, phase)) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -909,9 +981,9 @@ template <class T> struct Cycle {
   void level_op(int l, int op, int a, int b, int c) {
     const double bytes = level_op_bytes(D, l, op, b, c, sizeof(T));
     if (few_rows(l))
-      probed(kProbeRows, s, bytes, [&] { k_mgl_rows<T><<<rows_grid(l), NT, 0, s>>>(D, phase, op, l, a, b, c); });
+      probed(kProbeRows, s, bytes, [&] { pdl_launch((k_mgl_rows<T>), rows_grid(l), NT, 0, s, D, phase, op, l, a, b, c); });
     else
-      probed(kProbeRowThread, s, bytes, [&] { k_mgl<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, phase, op, l, a, b, c); });
+      probed(kProbeRowThread, s, bytes, [&] { pdl_launch((k_mgl<T>), grid_for(D.lv[l].count), NT, 0, s, D, phase, op, l, a, b, c); });
   }
   dim3 grid0() const { return dim3((unsigned)((D.nx + kTileX - 1) / kTileX), (unsigned)((D.ny + kTileY - 1) / kTileY), (unsigned)D.nz); }
   int smooth(int l, int field, bool zero, bool last0) {
@@ -926,12 +998,12 @@ template <class T> struct Cycle {
       if (D.mg_smoother == 1) {
         if (l == 0)
           probed(kProbeSmooth0, s, smooth0_bytes(D, phase, sweep + 1, first ? 1 : 0, fin ? 1 : -1, sizeof(T)), [&] {
-            k_mg0_cheb<T><<<grid0(), NT, 0, s>>>(D, phase, field, cheb_c1(sweep + 1), cheb_c2(sweep + 1), sweep == 0 ? 1 : 0,
+            pdl_launch((k_mg0_cheb<T>), grid0(), NT, 0, s, D, phase, field, cheb_c1(sweep + 1), cheb_c2(sweep + 1), sweep == 0 ? 1 : 0,
                                                  first ? 1 : 0, fin ? 1 : -1);
           });
         else level_op(l, 0, field, sweep + 1, first ? 1 : 0);
       } else if (l == 0)
-        k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 1, l, field, first ? 1 : 0, 0);
+        pdl_launch((k_mgl<T>), gr, NT, 0, s, D, phase, 1, l, field, first ? 1 : 0, 0);
       else
         level_op(l, 1, field, first ? 1 : 0, 0);
       field = 3 - field;
@@ -943,7 +1015,10 @@ template <class T> struct Cycle {
   int level(int l) {
     unsigned gr = grid_for(D.lv[l].count);
     if (l == D.L - 1 || l == D.mg_bottom) {
-      k_mg_bottom<T><<<1, 1024, 0, s>>>(D, phase, l);
+      if (D.mg_bottom_smem > 0 && l == D.mg_bottom)
+        pdl_launch((k_mg_bottom_smem<T>), 1, 1024, D.mg_bottom_smem, s, D, phase, l);
+      else
+        pdl_launch((k_mg_bottom<T>), 1, 1024, 0, s, D, phase, l);
       if (l == D.L - 1) {
         if (D.lv[l].count <= 64) return 1;
         return 1;  // 32 Jacobi sweeps end in field 1
@@ -951,24 +1026,25 @@ template <class T> struct Cycle {
       return bottom_field();
     }
     int field = smooth(l, 1, true, false);
-    if (l == 0) k_mg0_residual<T><<<grid0(), NT, 0, s>>>(D, phase, field);
+    if (l == 0) pdl_launch((k_mg0_residual<T>), grid0(), NT, 0, s, D, phase, field);
     else level_op(l, 2, field, 0, 0);
-    k_mgl<T><<<grid_for(D.lv[l + 1].count), NT, 0, s>>>(D, phase, 3, l + 1, 0, 0, 0);
+    pdl_launch((k_mgl<T>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, 3, l + 1, 0, 0, 0);
     int cf = level(l + 1);
-    k_mgl<T><<<gr, NT, 0, s>>>(D, phase, 4, l, field, cf, 0);
+    pdl_launch((k_mgl<T>), gr, NT, 0, s, D, phase, 4, l, field, cf, 0);
     return smooth(l, field, false, l == 0 && D.mg_smoother == 1);
   }
   void run() {
-    if (phase == 0) k_mg0_load<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, D.mg_smoother == 1 ? 1 : 0);
+    if (phase == 0) pdl_launch((k_mg0_load<T>), grid_for(D.N), NT, 0, s, D, phase, D.mg_smoother == 1 ? 1 : 0);
     fused_first = D.mg_smoother == 1;
     int f = level(0);
     // Chebyshev smoothing fuses z and the finalisation into the last level-0 sweep
-    if (D.mg_smoother != 1) k_mg_finish<T><<<grid_for(D.N), NT, 0, s>>>(D, phase, f);
+    if (D.mg_smoother != 1) pdl_launch((k_mg_finish<T>), grid_for(D.N), NT, 0, s, D, phase, f);
   }
 };
 
 // Columns of the ELL rows, max(wrap(l, q + offset), 0), computed once (static geometry).
 __global__ void __launch_bounds__(NT) k_mg_cols(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
   int i = blockIdx.x * NT + threadIdx.x;
@@ -983,6 +1059,7 @@ __global__ void __launch_bounds__(NT) k_mg_cols(const __grid_constant__ Dev D, i
 // Level-0 neighbour-active bits (bit f: neighbour across face f active, bit 6: cell active),
 // rebuilt after the masks on structural rebuilds.
 template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!build_on(D) || D.hstate[9] == 0) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -996,14 +1073,14 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(const __grid_c
 }
 
 template <class T> void build(const Dev& D, cudaStream_t s) {
-  k_hs_reset<<<1, 1, 0, s>>>(D);
-  k_hs_count<<<grid_for(D.N), NT, 0, s>>>(D);
-  k_hs_decide<<<1, 1, 0, s>>>(D);
-  k_hs_snapshot<T><<<grid_for(D.N), NT, 0, s>>>(D);
-  for (int l = 0; l < D.L; l++) k_mg_mask<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
-  k_mg_nb0<T><<<grid_for(D.N), NT, 0, s>>>(D);
-  for (int l = 0; l + 1 < D.L; l++) k_mg_transfer<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
-  k_mg_scale<T><<<grid_for(D.lv[0].count), NT, 0, s>>>(D, 0);
+  pdl_launch(k_hs_reset, 1, 1, 0, s, D);
+  pdl_launch(k_hs_count, grid_for(D.N), NT, 0, s, D);
+  pdl_launch(k_hs_decide, 1, 1, 0, s, D);
+  pdl_launch((k_hs_snapshot<T>), grid_for(D.N), NT, 0, s, D);
+  for (int l = 0; l < D.L; l++) pdl_launch((k_mg_mask<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+  pdl_launch((k_mg_nb0<T>), grid_for(D.N), NT, 0, s, D);
+  for (int l = 0; l + 1 < D.L; l++) pdl_launch((k_mg_transfer<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+  pdl_launch((k_mg_scale<T>), grid_for(D.lv[0].count), NT, 0, s, D, 0);
   for (int l = 1; l < D.L; l++) {
     int lo, ext[3];
     // the children box extents of fine level l-1 are the same for every coarse row
@@ -1017,20 +1094,22 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
     (void)lo;
     int G = ext[1] * ext[2], rpb = GT / G;
     unsigned gr = (unsigned)((D.lv[l].count + rpb - 1) / rpb);
-    k_mg_galerkin<T><<<gr, GT, 125 * GT * sizeof(float), s>>>(D, l - 1, ext[0], ext[1], ext[2]);
-    k_mg_scale<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+    pdl_launch((k_mg_galerkin<T>), gr, GT, 125 * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
+    pdl_launch((k_mg_scale<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   }
-  for (int l = 1; l < D.L; l++) k_mg_ell<T><<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
-  if (D.lv[D.L - 1].count <= 64) k_mg_chol<T><<<1, 64, 0, s>>>(D, D.L - 1);
-  k_hs_record<<<1, 1, 0, s>>>(D);
+  for (int l = 1; l < D.L; l++) pdl_launch((k_mg_ell<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+  if (D.lv[D.L - 1].count <= 64) pdl_launch((k_mg_chol<T>), 1, 64, 0, s, D, D.L - 1);
+  pdl_launch(k_hs_record, 1, 1, 0, s, D);
 }
 
 }  // namespace
 
 void launch_mg_cols(const Dev& D, cudaStream_t s) {
-  for (int l = 1; l < D.L; l++) k_mg_cols<<<grid_for(D.lv[l].count), NT, 0, s>>>(D, l);
+  for (int l = 1; l < D.L; l++) pdl_launch(k_mg_cols, grid_for(D.lv[l].count), NT, 0, s, D, l);
 }
 void mg_kernel_attributes() {
+  cudaFuncSetAttribute(k_mg_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
+  cudaFuncSetAttribute(k_mg_bottom_smem<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
   cudaFuncSetAttribute(k_mg_galerkin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
   cudaFuncSetAttribute(k_mg_galerkin<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));
 }

@@ -78,6 +78,7 @@ DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
 // which 0: the accepted time and the CFL look-ahead time (before op 20); which 1: the new time
 // c1 + dt and the relaxation factors at dt (after op 20 has set dt).  One thread per (column, row).
 __global__ void __launch_bounds__(NT) k_wave_tables(const __grid_constant__ Dev D, int which) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   const Grid g(D);
   const Coast cs(D);
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(NT) k_wave_tables(const __grid_constant__ Dev 
 
 // ---------------------------------------------------------------- op 20/21
 __global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -128,6 +130,7 @@ __global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- op 45/46 + c_i of op 22
 __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Motion m(D);
   const float* pmA = m.acc == 0 ? D.pmask0 : D.pmask1;
@@ -160,6 +163,7 @@ __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) 
 
 // ---------------------------------------------------------------- op 23
 __global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -200,6 +204,7 @@ DI float sweep_flux(const Motion& m, I3 q, int axis) {
 
 // ---------------------------------------------------------------- op 24 + 55/56 + 25/26
 __global__ void __launch_bounds__(NT) k_sweep_update(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Motion m(D);
   int sa = ((int)D.c[2] + (int)D.c[21]) % 3;
@@ -486,17 +491,43 @@ DI F3 face_x(const Dev& D, const Grid& g, I3 q, int axis) {
   return x;
 }
 // cached_advection, forward pass (coupled_motion.glslinc:170-179); dbg (optional) gets 16 floats.
+// The nine samples (three components at x, at the midpoint and at the end point) come from one
+// sampler call site in a loop that is not unrolled, so the sampler is emitted once per kernel.
 DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float* dbg) {
   const Dev& D = mc.m.D;
-  long long nf = D.NF;
-  bool vs, vm, ve;
-  float l0, l1v;
-  F3 sv = mc.velocity_checked(x, vs);
-  float hd = .5f * d;
-  F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
-  F3 s2 = mc.velocity_checked(mid, vm);
-  F3 end = mf(x.x - d * s2.x, x.y - d * s2.y, x.z - d * s2.z);
-  float value = mc.endpoint(end, axis, false, ve, l0, l1v);
+  const long long nf = D.NF;
+  const float hd = .5f * d;
+  F3 p = x, sv = mf(0.f, 0.f, 0.f), mid = x, end = x;
+  float value = 0.f, l0 = 0.f, l1v = 0.f;
+  unsigned ok = 7u;  // bit s: every sample of stage s supported
+#pragma unroll 1
+  for (int stage = 0; stage < 3; stage++) {
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+#pragma unroll 1
+    for (int a = 0; a < 3; a++) {
+      bool valid;
+      float lo, hi;
+      const float s = mc.sample(p, a, false, valid, lo, hi);
+      if (!valid) ok &= ~(1u << stage);
+      if (a == 0) v0 = s;
+      else if (a == 1) v1 = s;
+      else v2 = s;
+      if (stage == 2 && a == axis) {
+        value = s;
+        l0 = lo;
+        l1v = hi;
+      }
+    }
+    if (stage == 0) {
+      sv = mf(v0, v1, v2);
+      mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
+      p = mid;
+    } else if (stage == 1) {
+      end = mf(x.x - d * v0, x.y - d * v1, x.z - d * v2);
+      p = end;
+    }
+  }
+  const bool vs = ok & 1u, vm = ok & 2u, ve = ok & 4u;
   bool clear = !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end);
   if (dbg) {
     float t[16] = {x.x, x.y, x.z, sv.x, sv.y, sv.z, (float)vs, mid.x, mid.y, mid.z, (float)vm, end.x, end.y, end.z, (float)ve, (float)clear};
@@ -511,23 +542,41 @@ DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float*
   D.tcache[5 * nf + i] = sv.z;
   return value;
 }
-// cached_advection, corrected pass (coupled_motion.glslinc:180-187)
+// cached_advection, corrected pass (coupled_motion.glslinc:180-187): the reverse trace from the
+// cached start velocity, six samples from one call site.
 DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
   const Dev& D = mc.m.D;
-  long long nf = D.NF;
-  float forward = D.fwd[i];
+  const long long nf = D.NF;
+  const float forward = D.fwd[i];
   if (D.tcache[2 * nf + i] < .5f) return forward;
-  F3 sv = mf(D.tcache[3 * nf + i], D.tcache[4 * nf + i], D.tcache[5 * nf + i]);
-  bool vm, ve;
-  float u0, u1;
-  float rd = -d;
-  float hd = .5f * rd;
-  F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
-  F3 s2 = mc.velocity_checked(mid, vm);
-  F3 end = mf(x.x - rd * s2.x, x.y - rd * s2.y, x.z - rd * s2.z);
-  float backward = mc.endpoint(end, axis, true, ve, u0, u1);
+  const F3 sv = mf(D.tcache[3 * nf + i], D.tcache[4 * nf + i], D.tcache[5 * nf + i]);
+  const float rd = -d;
+  const float hd = .5f * rd;
+  const F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
+  F3 p = mid, end = mid;
+  float backward = 0.f;
+  bool ok = true;
+#pragma unroll 1
+  for (int stage = 0; stage < 2; stage++) {
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+#pragma unroll 1
+    for (int a = 0; a < 3; a++) {
+      bool valid;
+      float lo, hi;
+      const float s = mc.sample(p, a, stage == 1 && a == axis, valid, lo, hi);
+      ok = ok && valid;
+      if (a == 0) v0 = s;
+      else if (a == 1) v1 = s;
+      else v2 = s;
+      if (stage == 1 && a == axis) backward = s;
+    }
+    if (stage == 0) {
+      end = mf(x.x - rd * v0, x.y - rd * v1, x.z - rd * v2);
+      p = end;
+    }
+  }
   float corrected = forward + .5f * (mc.m.A[D.N + i] - backward);
-  return (vm && ve && !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end) && corrected >= D.tcache[i] &&
+  return (ok && !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end) && corrected >= D.tcache[i] &&
           corrected <= D.tcache[nf + i])
              ? corrected
              : forward;
@@ -567,9 +616,11 @@ template <int op, bool cached> DI void mac_face(const Dev& D, const Motion& m, c
 // warp appends its faces contiguously.  A face that does not advect gets its op 27/28 results
 // (zero) here.  mac_ctr: [0] interior count, [1] boundary count, [2]/[3] op 27/28 work cursors.
 __global__ void k_mac_reset(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (threadIdx.x < 4) D.mac_ctr[threadIdx.x] = 0u;
 }
 __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   Motion m(D);
   const float* vb = m.acc == 0 ? D.vband0 : D.vband1;
@@ -604,6 +655,7 @@ __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) 
 // Persistent pass over the work list: each warp takes 32 consecutive entries at a time, boundary
 // faces first, so a slow warp never holds idle lanes of a finished block.
 template <int op, bool cached> __global__ void __launch_bounds__(NT) k_mac(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!setup_on(D)) return;
   const unsigned n_int = D.mac_ctr[0], n_edge = D.mac_ctr[1], total = n_int + n_edge;
   unsigned* cursor = D.mac_ctr + (op == 27 ? 2 : 3);
@@ -675,15 +727,15 @@ void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis,
 
 void launch_motion_cfl(const Dev& D, cudaStream_t s) {
   const unsigned wt = grid_for((long long)D.wt_w * D.wt_h);
-  if (D.coastal) k_wave_tables<<<wt, NT, 0, s>>>(D, 0);
-  k_cfl<<<grid_for(D.N), NT, 0, s>>>(D);
-  if (D.coastal) k_wave_tables<<<wt, NT, 0, s>>>(D, 1);
-  k_compress<<<grid_for(D.N), NT, 0, s>>>(D);
+  if (D.coastal) pdl_launch(k_wave_tables, wt, NT, 0, s, D, 0);
+  pdl_launch(k_cfl, grid_for(D.N), NT, 0, s, D);
+  if (D.coastal) pdl_launch(k_wave_tables, wt, NT, 0, s, D, 1);
+  pdl_launch(k_compress, grid_for(D.N), NT, 0, s, D);
 }
 void launch_sweep(const Dev& D, cudaStream_t s) {
-  k_sweep_plane<<<grid_for(D.N), NT, 0, s>>>(D);
+  pdl_launch(k_sweep_plane, grid_for(D.N), NT, 0, s, D);
   // reads F, the plane field (16 B), the sweep-axis faces and c_i; writes F
-  probed(kProbeSweepVof, s, 32.0 * (double)D.N, [&] { k_sweep_update<<<grid_for(D.N), NT, 0, s>>>(D); });
+  probed(kProbeSweepVof, s, 32.0 * (double)D.N, [&] { pdl_launch(k_sweep_update, grid_for(D.N), NT, 0, s, D); });
 }
 int mac_blocks() {
   int dev = 0, sms = 0, per_sm = 0;
@@ -693,17 +745,17 @@ int mac_blocks() {
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 void launch_maccormack(const Dev& D, cudaStream_t s) {
-  k_mac_reset<<<1, 32, 0, s>>>(D);
-  k_mac_list<<<grid_for(D.NF), NT, 0, s>>>(D);
+  pdl_launch(k_mac_reset, 1, 32, 0, s, D);
+  pdl_launch(k_mac_list, grid_for(D.NF), NT, 0, s, D);
   // op 27 reads the accepted faces and valid band, writes the forward values (and, with the trace
   // cache, its six fields); op 28 reads those, the faces and the band, and writes the candidate.
   const double nf = (double)D.NF, cache = (D.flags & 4) ? 6.0 : 0.0;
   if (D.flags & 4) {
-    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { k_mac<27, true><<<D.mac_grid, NT, 0, s>>>(D); });
-    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { k_mac<28, true><<<D.mac_grid, NT, 0, s>>>(D); });
+    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true>), D.mac_grid, NT, 0, s, D); });
+    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true>), D.mac_grid, NT, 0, s, D); });
   } else {
-    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { k_mac<27, false><<<D.mac_grid, NT, 0, s>>>(D); });
-    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { k_mac<28, false><<<D.mac_grid, NT, 0, s>>>(D); });
+    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, false>), D.mac_grid, NT, 0, s, D); });
+    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, false>), D.mac_grid, NT, 0, s, D); });
   }
 }
 

@@ -36,6 +36,7 @@ namespace {
 
 // ---------------------------------------------------------------- op 3 (+ op 4 when the V-cycle is off)
 __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!pressure_setup(D)) return;
   Grid g(D);
   const float* Cb = bank_ptr(D, 1 - acc_bank(D));
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- op 5 + 6 + 7
 __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!solving(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -97,6 +99,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- op 8 + multigrid load (op 5 of the cycle)
 template <class T> __global__ void __launch_bounds__(NT) k_cg_update(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   if (!solving(D)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -121,6 +124,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_cg_update(const __gri
 
 // ---------------------------------------------------------------- op 10 (+ loop condition)
 __global__ void __launch_bounds__(NT) k_cg_direction(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int use_handle) {
+  grid_dep_wait();
   bool on = solving(D);
   if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) {
     // The body has run ops 5-10 of one iteration; continue while solving.
@@ -135,6 +139,7 @@ __global__ void __launch_bounds__(NT) k_cg_direction(const __grid_constant__ Dev
 
 // ---------------------------------------------------------------- graph conditions
 __global__ void k_set_cond(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int which) {
+  grid_dep_wait();
   const double* c = D.c;
   bool v;
   if (which == kCondDefectFirst) v = true;
@@ -146,6 +151,7 @@ __global__ void k_set_cond(const __grid_constant__ Dev D, cudaGraphConditionalHa
 
 // ---------------------------------------------------------------- ops 43 + 1 (trial begin) and 63/64
 __global__ void k_begin(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   double* c = D.c;
   // op 43 (coupled_motion.glslinc:351-355)
   bool retry = c[7] == 20 || (c[7] >= 10 && c[7] <= 12);
@@ -162,6 +168,7 @@ __global__ void k_begin(const __grid_constant__ Dev D) {
   }
 }
 __global__ void __launch_bounds__(NT) k_defect_begin(const __grid_constant__ Dev D) {
+  grid_dep_wait();
   const double* c = D.c;
   double c57 = c[57];
   bool go = (c57 == 1 || c57 == 2) && c[7] < .5;
@@ -184,19 +191,29 @@ __global__ void __launch_bounds__(NT) k_defect_begin(const __grid_constant__ Dev
 
 static unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
 
-void launch_begin(const Dev& D, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(D); }
-void launch_defect_begin(const Dev& D, cudaStream_t s) { k_defect_begin<<<grid_for(D.N), NT, 0, s>>>(D); }
-void launch_cg_init(const Dev& D, cudaStream_t s) { k_cg_init<<<grid_for(D.N), NT, 0, s>>>(D); }
-void launch_cg_matvec(const Dev& D, cudaStream_t s) { k_cg_matvec<<<grid_for(D.N), NT, 0, s>>>(D); }
+void launch_begin(const Dev& D, cudaStream_t s) { pdl_launch(k_begin, 1, 1, 0, s, D); }
+void launch_defect_begin(const Dev& D, cudaStream_t s) { pdl_launch(k_defect_begin, grid_for(D.N), NT, 0, s, D); }
+void launch_cg_init(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_init, grid_for(D.N), NT, 0, s, D); }
+void launch_cg_matvec(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_matvec, grid_for(D.N), NT, 0, s, D); }
 void launch_cg_update(const Dev& D, cudaStream_t s) {
-  if (D.bf16) k_cg_update<__nv_bfloat16><<<grid_for(D.N), NT, 0, s>>>(D);
-  else k_cg_update<float><<<grid_for(D.N), NT, 0, s>>>(D);
+  if (D.bf16) pdl_launch((k_cg_update<__nv_bfloat16>), grid_for(D.N), NT, 0, s, D);
+  else pdl_launch((k_cg_update<float>), grid_for(D.N), NT, 0, s, D);
 }
 void launch_cg_direction(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int use_handle) {
-  k_cg_direction<<<grid_for(D.N), NT, 0, s>>>(D, h, use_handle);
+  pdl_launch(k_cg_direction, grid_for(D.N), NT, 0, s, D, h, use_handle);
 }
 void launch_set_cond(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int which) {
-  k_set_cond<<<1, 1, 0, s>>>(D, h, which);
+  pdl_launch(k_set_cond, 1, 1, 0, s, D, h, which);
 }
+
+// Holds the stream for a fixed number of SM clock cycles (kernel probes only: while it runs the
+// host enqueues the next batch, so the probed launches then run back to back).  Bounded by its
+// cycle count; it waits on nothing else.
+__global__ void k_delay(long long cycles) {
+  const long long t0 = clock64();
+  while (clock64() - t0 < cycles) {
+  }
+}
+void launch_delay(cudaStream_t s, long long cycles) { k_delay<<<1, 1, 0, s>>>(cycles); }
 
 }  // namespace wg

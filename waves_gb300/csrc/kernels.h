@@ -10,6 +10,26 @@ namespace wg {
 
 enum CondKind { kCondActive = 0, kCondSolving = 1, kCondDefect = 2, kCondDefectFirst = 3 };
 
+// Programmatic dependent launch: a kernel launched this way may be scheduled while the previous
+// kernel on the stream drains; every kernel's first statement is grid_dep_wait()
+// (griddepcontrol.wait), which returns once that kernel has completed and its writes are visible,
+// so only launch latency overlaps.  On by default; WAVES_PDL=0 at handle creation turns it off.
+extern bool g_pdl;
+template <class... KArgs, class... Args>
+void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // Kernel probes.  While a probe list is installed on the calling thread (host-scheduled trials
 // only, never during graph capture), each probed launch site brackets its launch with two events
 // on its stream and records the launch's algorithmic bytes: the distinct input arrays read once
@@ -51,6 +71,7 @@ void launch_cg_matvec(const Dev& D, cudaStream_t s);
 void launch_cg_update(const Dev& D, cudaStream_t s);
 void launch_cg_direction(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int use_handle);
 void launch_set_cond(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int which);
+void launch_delay(cudaStream_t s, long long cycles);
 // k_motion.cu
 void launch_motion_cfl(const Dev& D, cudaStream_t s);
 void launch_sweep(const Dev& D, cudaStream_t s);

@@ -28,6 +28,7 @@ using wg::Dev;
 
 namespace wg {
 thread_local std::vector<ProbeRec>* g_probe = nullptr;
+bool g_pdl = true;
 }
 
 namespace {
@@ -487,6 +488,15 @@ waves_status setup_device(waves_handle* h) {
   // Levels with fewer rows than this use the product-parallel apply (both forms give the same bits).
   D.mg_rows_below = 65536;
   if (const char* e = getenv("WAVES_MG_ROWS_BELOW")) D.mg_rows_below = std::max(0, atoi(e));
+  {
+    // levels mg_bottom..L-1 staged in shared memory when their fields and rows fit
+    const int lb = D.mg_bottom, Lc = D.L - 1;
+    const size_t span = (size_t)D.lv[Lc].off + D.lv[Lc].count - D.lv[lb].off;
+    const size_t rows = (size_t)(D.lv[Lc].eoff + (long long)D.lv[Lc].stencil * D.lv[Lc].count - D.lv[lb].eoff);
+    const size_t bytes = ((8 * span * tsz + 15) & ~(size_t)15) + rows * tsz;
+    D.mg_bottom_smem = lb >= 1 && bytes <= (size_t)wg::kBottomSmemMax ? (int)bytes : 0;
+    if (getenv("WAVES_MG_BOTTOM_GLOBAL")) D.mg_bottom_smem = 0;
+  }
   AL(D.mgmat, moff, true, "mg_matrix");
   {
     void* p;
@@ -703,19 +713,28 @@ waves_status upload_quota(waves_handle* h) {
 waves_status host_trial(waves_handle* h, int batch = 4) {
   const Dev& D = h->D;
   cudaStream_t s = h->stream;
+  // with kernel probes installed, each batch starts behind a fixed delay (~2 ms) so that the
+  // host has enqueued the batch before the GPU reaches it
+  auto hold = [&] {
+    if (wg::g_probe) wg::launch_delay(s, 4000000LL);
+  };
   wg::launch_begin(D, s);
   waves_status st;
   if ((st = read_control(h)) != WAVES_OK) return st;
   if (!(h->host_c[4] > .5)) return WAVES_OK;
+  hold();
   enqueue_setup(h, s);
-  while (true) {
+  for (int round = 0;; round++) {
+    if (round > 0) hold();
     enqueue_cg_begin(h, s);
     if ((st = read_control(h)) != WAVES_OK) return st;
     const double* c = h->host_c;
     while (c[4] > .5 && c[6] < .5 && c[7] < .5) {
+      hold();
       for (int k = 0; k < batch; k++) enqueue_cg_iteration(h, s, 0, 0);
       if ((st = read_control(h)) != WAVES_OK) return st;
     }
+    hold();
     wg::launch_post(D, s);
     if ((st = read_control(h)) != WAVES_OK) return st;
     if (!(c[57] == 1 && c[7] < .5 && c[4] > .5)) break;
@@ -754,6 +773,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
   }
   waves_handle* h = new waves_handle;
   h->cfg = *cfg;
+  if (const char* e = getenv("WAVES_PDL")) wg::g_pdl = atoi(e) != 0;
   waves_status st = WAVES_OK;
   auto fail = [&](waves_status s) {
     g_create_error = h->err;
