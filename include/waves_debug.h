@@ -5,7 +5,8 @@
  * phases are, in trial order: 0 begin (ops 43, 1), 1 CFL and compression pre-check, 2 one VOF
  * sweep, 3 MacCormack, 4 coastal forcing, 5 geometry, 6 projection set-up, 7 multigrid build,
  * 8 CG set-up with the first V-cycle, 9 one CG iteration, 10 projection, extension and
- * acceptance, 11 trial end.  waves_debug_read copies a named device array (the names of the
+ * acceptance, 11 trial end; 12 is the learned warm start, which a trial runs between phases 6
+ * and 7 when it is configured.  waves_debug_read copies a named device array (the names of the
  * allocations in waves_abi.cu) to host memory.
  */
 #ifndef WAVES_DEBUG_H

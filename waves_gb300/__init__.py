@@ -126,6 +126,35 @@ class WavesSolver:
         arr = np.ascontiguousarray(c, dtype=np.float64)
         self._ck(self.lib.waves_set_control(self.h, arr.ctypes.data_as(C.POINTER(C.c_double)), len(arr)))
 
+    def set_warm_start(self, weights=None, biases=None, input_scale=(1.0, 1.0, 1.0), output_scale=1.0):
+        """Load the warm-start network (waves_set_warm_start): weights[l] are BF16 bit patterns
+        laid out [co][kz][ky][kx][ci] (channels 3, 16, 16, 16 in; 16, 16, 16, 1 out), biases[l]
+        FP32; None turns the learned start off."""
+        from .abi import WAVES_NET_LAYERS, WavesWarmStartModel
+        if weights is None:
+            self._ck(self.lib.waves_set_warm_start(self.h, None))
+            return
+        m = WavesWarmStartModel()
+        keep = []
+        for l in range(WAVES_NET_LAYERS):
+            w = np.ascontiguousarray(weights[l], dtype=np.uint16).ravel()
+            b = np.ascontiguousarray(biases[l], dtype=np.float32).ravel()
+            keep += [w, b]
+            m.weights[l] = w.ctypes.data_as(C.POINTER(C.c_uint16))
+            m.bias[l] = b.ctypes.data_as(C.POINTER(C.c_float))
+        for k in range(3):
+            m.input_scale[k] = float(input_scale[k])
+        m.output_scale = float(output_scale)
+        self._ck(self.lib.waves_set_warm_start(self.h, C.byref(m)))
+
+    def debug_phase(self, phase):
+        self._ck(self.lib.waves_debug_phase(self.h, int(phase)))
+
+    def debug_read(self, name, count, dtype=np.float32):
+        out = np.empty(count, dtype=dtype)
+        self._ck(self.lib.waves_debug_read(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
     def probe_trial(self):
         """Run one host-scheduled trial with kernel probes (waves_debug_probe_trial): per probed
         kernel, launches, summed CUDA-event milliseconds and summed algorithmic bytes."""

@@ -21,7 +21,10 @@ enum CtrlExtra {
   kQuota = 101,         // request quota (>= 0 steps, < 0 minus a deadline)
   kWarmUsed = 102,      // trials started from the learned warm start
   kDefectRounds = 103,  // defect-correction rounds run since creation
+  kNetLoaded = 104,     // 1 once a warm-start network is loaded
+  kWarmPick = 105,      // 1 when this trial starts from the network's pressure
 };
+constexpr int kNetLayerWords = 27 * 2 * 64;  // mma fragments of one layer's weights (uint32)
 
 struct MGLevelDev {
   int nx, ny, nz, count;
@@ -110,6 +113,14 @@ struct Dev {
   int* mac_list;                 // MacCormack work list (faces)
   unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
   int mac_grid;                  // persistent MacCormack blocks
+  // learned warm start (allocated when warm_start is configured): weights in mma fragment order,
+  // biases [4][16], scales (F, b, p_prev inputs; output), BF16 activations [2][N][16], p_net [N]
+  int net_on;
+  uint32_t* net_w;
+  float* net_b;
+  float* net_scale;
+  unsigned short* net_act;
+  float* net_p;
   int tab_w, tab_h;
 
   // multigrid
@@ -152,6 +163,7 @@ enum Site {
   kSiteRZ,
   kSiteAccept,
   kSiteHS,
+  kSiteWarm,
   kSiteCount
 };
 

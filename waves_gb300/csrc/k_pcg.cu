@@ -30,6 +30,60 @@ DI float operator_at(const Dev& D, const Grid& g, I3 q, long long i, const float
   return result;
 }
 
+// ---------------------------------------------------------------- learned warm start
+DI bool warm_on(const Dev& D) { return D.c[kNetLoaded] > .5 && D.c[5] > .5 && D.c[7] < .5; }
+// b of op 3 (pressure_iterations.glslinc) ahead of the network, the same expression as k_cg_init
+__global__ void __launch_bounds__(NT) k_warm_rhs(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  if (!warm_on(D)) return;
+  Grid g(D);
+  const float* Cb = bank_ptr(D, 1 - acc_bank(D));
+  float dt = (float)D.c[20];
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  float bv = 0.f;
+  if (D.kind[i] > 0) {
+    I3 q = g.coord(i);
+    float dv = 0.f;
+    for (int axis = 0; axis < 3; axis++) {
+      I3 right = ax(q, axis, 1);
+      dv += (Cb[g.face_index(right, axis)] - Cb[g.face_index(q, axis)]) / g.h(axis);
+    }
+    bv = -1000.0f / dt * dv;
+  }
+  D.b[i] = bv;
+}
+// |b - A p_prev|^2 and |b - A p_net|^2 over wet cells (FP64); the network's pressure is taken
+// only when its residual is smaller, so plain MGPCG stays the fallback.
+__global__ void __launch_bounds__(NT) k_warm_decide(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  if (!warm_on(D)) return;
+  Grid g(D);
+  const float* p = bank_ptr(D, 1 - acc_bank(D)) + D.N + D.NF;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  double v[2] = {0, 0};
+  if (i < D.N && D.kind[i] > 0) {
+    I3 q = g.coord(i);
+    const float rp = D.b[i] - operator_at(D, g, q, i, p), rn = D.b[i] - operator_at(D, g, q, i, D.net_p);
+    v[0] = (double)rp * (double)rp;
+    v[1] = (double)rn * (double)rn;
+  }
+  const int ops[2] = {0, 0};
+  double out[2];
+  if (last_block_reduce<NT, 2>(D, kSiteWarm, v, ops, out) && threadIdx.x == 0) {
+    const bool pick = out[1] < out[0];
+    D.c[kWarmPick] = pick ? 1.0 : 0.0;
+    if (pick) D.c[kWarmUsed] += 1;
+  }
+}
+__global__ void __launch_bounds__(NT) k_warm_apply(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  if (!warm_on(D) || !(D.c[kWarmPick] > .5)) return;
+  long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i >= D.N) return;
+  bank_ptr(D, 1 - acc_bank(D))[D.N + D.NF + i] = D.net_p[i];
+}
+
 }  // namespace
 
 namespace {
@@ -193,6 +247,13 @@ static unsigned grid_for(long long n) { return (unsigned)((n + NT - 1) / NT); }
 
 void launch_begin(const Dev& D, cudaStream_t s) { pdl_launch(k_begin, 1, 1, 0, s, D); }
 void launch_defect_begin(const Dev& D, cudaStream_t s) { pdl_launch(k_defect_begin, grid_for(D.N), NT, 0, s, D); }
+void launch_warm_start(const Dev& D, cudaStream_t s) {
+  if (!D.net_on) return;
+  pdl_launch(k_warm_rhs, grid_for(D.N), NT, 0, s, D);
+  launch_warm_network(D, s);
+  pdl_launch(k_warm_decide, grid_for(D.N), NT, 0, s, D);
+  pdl_launch(k_warm_apply, grid_for(D.N), NT, 0, s, D);
+}
 void launch_cg_init(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_init, grid_for(D.N), NT, 0, s, D); }
 void launch_cg_matvec(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_matvec, grid_for(D.N), NT, 0, s, D); }
 void launch_cg_update(const Dev& D, cudaStream_t s) {

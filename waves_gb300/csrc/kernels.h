@@ -67,6 +67,9 @@ template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launc
 void launch_begin(const Dev& D, cudaStream_t s);
 void launch_defect_begin(const Dev& D, cudaStream_t s);
 void launch_cg_init(const Dev& D, cudaStream_t s);
+void launch_warm_start(const Dev& D, cudaStream_t s);  // learned warm start after op 2 (no-op when not configured)
+// k_net.cu
+void launch_warm_network(const Dev& D, cudaStream_t s);
 void launch_cg_matvec(const Dev& D, cudaStream_t s);
 void launch_cg_update(const Dev& D, cudaStream_t s);
 void launch_cg_direction(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int use_handle);

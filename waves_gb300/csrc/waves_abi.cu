@@ -352,6 +352,14 @@ waves_status setup_device(waves_handle* h) {
     CK(cudaMemcpyAsync(D.wstamp, nan4, sizeof(nan4), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
   }
+  if (k.warm_start) {
+    D.net_on = 1;
+    AL(D.net_w, (size_t)WAVES_NET_LAYERS * wg::kNetLayerWords, false, "net_weights");
+    AL(D.net_b, (size_t)WAVES_NET_LAYERS * 16, false, "net_bias");
+    AL(D.net_scale, 4, false, "net_scale");
+    AL(D.net_act, (size_t)2 * N * 16, false, "net_activations");
+    AL(D.net_p, N, false, "net_pressure");
+  }
   AL(D.mac_list, NF, false, "mac_list");
   AL(D.mac_ctr, 4, false, "mac_counters");
   D.mac_grid = wg::mac_blocks();
@@ -534,6 +542,7 @@ void enqueue_pressure_setup(waves_handle* h, cudaStream_t s) {
   const Dev& D = h->D;
   wg::launch_geometry(D, s);
   wg::launch_proj_setup(D, s);
+  wg::launch_warm_start(D, s);
   wg::launch_mg_build(D, s);
 }
 void enqueue_setup(waves_handle* h, cudaStream_t s) {
@@ -1114,9 +1123,52 @@ waves_status waves_load(waves_handle* h, const void* buffer, size_t bytes) {
 
 waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model* model) {
   if (!h) return WAVES_INVALID_ARG;
-  (void)model;
-  h->err = "learned warm start not available in this build";
-  return WAVES_INVALID_ARG;
+  Dev& D = h->D;
+  if (!D.net_on) {
+    h->err = "the handle was created without warm_start = 1";
+    return WAVES_INVALID_ARG;
+  }
+  const double off = 0.0, on = 1.0;
+  if (!model) {  // back to the previous accepted pressure
+    CK(cudaMemcpyAsync(D.c + wg::kNetLoaded, &off, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return WAVES_OK;
+  }
+  const int ci_of[WAVES_NET_LAYERS] = {3, WAVES_NET_HIDDEN, WAVES_NET_HIDDEN, WAVES_NET_HIDDEN};
+  const int co_of[WAVES_NET_LAYERS] = {WAVES_NET_HIDDEN, WAVES_NET_HIDDEN, WAVES_NET_HIDDEN, 1};
+  for (int l = 0; l < WAVES_NET_LAYERS; l++)
+    if (!model->weights[l] || !model->bias[l]) {
+      h->err = "warm-start model with a missing layer";
+      return WAVES_INVALID_ARG;
+    }
+  // weights[co][kz][ky][kx][ci] (BF16 bits) -> mma.m16n8k16 B fragments [tap][n-tile][lane][2]:
+  // lane (g = lane / 4, t = lane % 4) holds output channel n = 8 j + g, input channels 2t, 2t + 1
+  // (first register) and 2t + 8, 2t + 9 (second), low half first; absent channels are zero.
+  std::vector<uint32_t> frag((size_t)WAVES_NET_LAYERS * wg::kNetLayerWords, 0u);
+  std::vector<float> bias((size_t)WAVES_NET_LAYERS * 16, 0.f);
+  for (int l = 0; l < WAVES_NET_LAYERS; l++) {
+    const int CI = ci_of[l], CO = co_of[l], tiles = CO > 8 ? 2 : 1;
+    auto w = [&](int co, int tap, int ci) -> uint32_t {
+      if (co >= CO || ci >= CI) return 0u;
+      return model->weights[l][((size_t)co * 27 + tap) * CI + ci];
+    };
+    for (int tap = 0; tap < 27; tap++)
+      for (int j = 0; j < tiles; j++)
+        for (int lane = 0; lane < 32; lane++) {
+          const int n = 8 * j + lane / 4, t = lane % 4;
+          const size_t at = (size_t)l * wg::kNetLayerWords + ((size_t)(tap * tiles + j) * 32 + lane) * 2;
+          frag[at] = w(n, tap, 2 * t) | (w(n, tap, 2 * t + 1) << 16);
+          frag[at + 1] = w(n, tap, 2 * t + 8) | (w(n, tap, 2 * t + 9) << 16);
+        }
+    for (int co = 0; co < CO; co++) bias[(size_t)l * 16 + co] = model->bias[l][co];
+  }
+  const float scale[4] = {model->input_scale[0], model->input_scale[1], model->input_scale[2], model->output_scale};
+  CK(cudaMemcpyAsync(D.net_w, frag.data(), frag.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(D.net_b, bias.data(), bias.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(D.net_scale, scale, sizeof(scale), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(D.c + wg::kNetLoaded, &on, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return WAVES_OK;
 }
 
 const char* waves_last_error(const waves_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
@@ -1139,6 +1191,7 @@ waves_status waves_debug_phase(waves_handle* h, int32_t phase) {
     case 9: enqueue_cg_iteration(h, s, 0, 0); break;
     case 10: wg::launch_post(D, s); break;
     case 11: wg::launch_trial_end(D, s); break;
+    case 12: wg::launch_warm_start(D, s); break;
     default: return WAVES_INVALID_ARG;
   }
   CK(cudaStreamSynchronize(s));

@@ -1,0 +1,211 @@
+"""Train the warm-start network on solve pairs captured from the solver, export it, evaluate it.
+
+    python -m waves_gb300.learned.train --seeds 8 --pairs 40 --out model.npz [--eval-seeds 2]
+
+Capture: for each seed the 310x48x80 beach (the lab settings) runs with a wave amplitude drawn
+from U(0.04, 0.10) m and a period from U(1.2, 1.8) s (wavenumber by the same dispersion
+bisection as the presets, std::mt19937_64-independent: numpy's PCG64 seeded with the seed).  It
+advances in the CUDA-graph path to the sampling times and takes one trial through the
+host-driven phases of include/waves_debug.h: after op 2 the candidate F and p_prev, after the CG
+set-up b, and at the first round's convergence (relative residual 1e-6) p*.
+
+Training (PyTorch, offline): the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
+ReLU, zero padding) maps (F, b * s_b, p_prev * s_p) to (p* - p_prev) / s_out on wet cells, with
+s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data; masked
+mean squared error on random 40x32x32 crops, scored away from the crop edge (the network's
+receptive field is 4 cells).  Export: BF16 weights [co][kz][ky][kx][ci], FP32 biases, the scales.
+
+Evaluation: held-out seeds run the same number of steps with and without the network; the
+result line gives CG iterations and pressure milliseconds per step for both.
+"""
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+import waves_gb300 as wg
+from waves_gb300.learned import CHANNELS, bf16_bits, load_model
+
+DEPTH = 0.45
+
+
+def beach(seed, warm=0):
+    rng = np.random.default_rng(seed)
+    amplitude, period = rng.uniform(0.04, 0.10), rng.uniform(1.2, 1.8)
+    cfg = wg.config("beach", pressure_tolerance=1e-6, warm_start=warm)
+    cfg.wave[0] = amplitude
+    cfg.wave[1] = wg.dispersion_k(period, DEPTH)
+    cfg.wave[2] = 2.0 * math.pi / period
+    cfg.wave[3] = DEPTH
+    return cfg, amplitude, period
+
+
+def capture_trial(s, N, NF):
+    """One trial through the debug phases; the first round's (F, b, p_prev, p*, kind) or None."""
+    s.debug_phase(0)
+    c = s.control()
+    if not c[4] > 0.5:
+        return None
+    for phase in (1, 2, 2, 2, 3, 4, 5, 6):
+        s.debug_phase(phase)
+    cand = 1 - int(c[0])
+    bank = s.bank(cand)
+    F, p_prev = bank[:N].copy(), bank[N + NF:N + NF + N].copy()
+    kind = s.geometry()[1].copy()
+    s.debug_phase(7)
+    pair, rounds = None, 0
+    while True:
+        s.debug_phase(8)
+        b = s.debug_read("b", N) if rounds == 0 else None
+        c = s.control()
+        while c[4] > 0.5 and c[6] < 0.5 and c[7] < 0.5:
+            s.debug_phase(9)
+            c = s.control()
+        if rounds == 0 and c[6] > 0.5 and c[7] < 0.5:
+            p_star = s.bank(cand)[N + NF:N + NF + N].copy()
+            pair = {"F": F, "b": b, "p_prev": p_prev, "p_star": p_star, "kind": kind}
+        s.debug_phase(10)
+        c = s.control()
+        rounds += 1
+        if not (c[57] == 1 and c[7] < 0.5 and c[4] > 0.5):
+            break
+    s.debug_phase(11)
+    return pair
+
+
+def capture(seeds, pairs, t0, gap):
+    out = []
+    for seed in seeds:
+        cfg, a, T = beach(seed)
+        s = wg.WavesSolver(cfg)
+        N, NF = s.N, s.NF
+        s.request_time(t0)
+        s.run()
+        for k in range(pairs):
+            s.request_time(t0 + (k + 1) * gap)
+            s.run()
+            s.request_steps(int(s.control()[2]) + 1)
+            p = capture_trial(s, N, NF)
+            if p is not None:
+                out.append(p)
+        s.close()
+        print(f"seed {seed}: a {a:.3f} m, T {T:.3f} s, {len(out)} pairs so far", flush=True)
+    return out
+
+
+def build_net(torch):
+    layers = []
+    for l, (ci, co) in enumerate(CHANNELS):
+        layers.append(torch.nn.Conv3d(ci, co, 3, padding=1))
+        if l < len(CHANNELS) - 1:
+            layers.append(torch.nn.ReLU())
+    return torch.nn.Sequential(*layers)
+
+
+def train(pairs, n, steps, seed, device):
+    import torch
+    torch.manual_seed(seed)
+    nx, ny, nz = n
+    grid = lambda a: torch.from_numpy(a.reshape(nz, ny, nx)).to(device)
+    wet = torch.stack([grid(p["kind"]) > 0 for p in pairs])
+    b = torch.stack([grid(p["b"]) for p in pairs])
+    pp = torch.stack([grid(p["p_prev"]) for p in pairs])
+    dp = torch.stack([grid(p["p_star"]) for p in pairs]) - pp
+    F = torch.stack([grid(p["F"]) for p in pairs])
+    s_b = 1.0 / max(float(b[wet].std()), 1e-12)
+    s_p = 1.0 / max(float(pp[wet].std()), 1e-12)
+    s_out = max(float(dp[wet].std()), 1e-12)
+    x = torch.stack([F, b * s_b, pp * s_p], dim=1)
+    y = (dp / s_out)[:, None]
+    m = wet[:, None].float()
+    net = build_net(torch).to(device)
+    opt = torch.optim.Adam(net.parameters(), lr=2e-3)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
+    cx, cy, cz, edge, batch = min(40, nx), min(32, ny), min(32, nz), 4, 8
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    t0 = time.time()
+    for step in range(steps):
+        idx = torch.randint(0, len(pairs), (batch,), generator=gen)
+        ox = torch.randint(0, nx - cx + 1, (batch,), generator=gen)
+        oy = torch.randint(0, ny - cy + 1, (batch,), generator=gen)
+        oz = torch.randint(0, nz - cz + 1, (batch,), generator=gen)
+        xs = torch.stack([x[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
+        ys = torch.stack([y[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
+        ms = torch.stack([m[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
+        e = (slice(None), slice(None), slice(edge, cz - edge), slice(edge, cy - edge), slice(edge, cx - edge))
+        pred = net(xs)
+        loss = ((pred - ys)[e] ** 2 * ms[e]).sum() / ms[e].sum().clamp(min=1.0)
+        opt.zero_grad()
+        loss.backward()
+        opt.step()
+        sched.step()
+        if step % max(steps // 10, 1) == 0 or step == steps - 1:
+            print(f"step {step}: masked MSE {loss.item():.4e} ({time.time() - t0:.1f} s)", flush=True)
+    with torch.no_grad():  # whole-field fit on the training pairs (fraction of variance left)
+        resid = sum(float((((net(x[i:i + 1]) - y[i:i + 1]) ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
+        total = sum(float(((y[i:i + 1] ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
+    convs = [mod for mod in net if isinstance(mod, torch.nn.Conv3d)]
+    weights = [bf16_bits(c.weight.detach().permute(0, 2, 3, 4, 1).contiguous().cpu().numpy()) for c in convs]
+    biases = [c.bias.detach().cpu().numpy().astype(np.float32) for c in convs]
+    return weights, biases, (1.0, s_b, s_p), s_out, resid / max(total, 1e-30)
+
+
+def evaluate(path, seeds, steps):
+    weights, biases, iscale, oscale = load_model(path)
+    rows = []
+    for seed in seeds:
+        row = {"seed": seed}
+        for warm in (0, 1):
+            cfg, a, T = beach(seed, warm)
+            s = wg.WavesSolver(cfg)
+            if warm:
+                s.set_warm_start(weights, biases, iscale, oscale)
+            s.request_time(1.0)
+            s.run()
+            c0 = s.control()
+            import ctypes as C
+            m_, p_, t_ = C.c_double(), C.c_double(), C.c_int64()
+            s.lib.waves_timing(s.h, C.byref(m_), C.byref(p_), C.byref(t_), 1)
+            s.request_steps(int(c0[2]) + steps)
+            s.run()
+            c1 = s.control()
+            s.lib.waves_timing(s.h, C.byref(m_), C.byref(p_), C.byref(t_), 1)
+            k = "learned" if warm else "plain"
+            row[k] = {"iters_per_step": (c1[18] - c0[18]) / steps, "pressure_ms_per_step": p_.value / steps,
+                      "warm_used": int(c1[102] - c0[102]), "trials": int(c1[32] - c0[32])}
+            s.close()
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--seeds", type=int, default=8)
+    ap.add_argument("--pairs", type=int, default=40)
+    ap.add_argument("--t0", type=float, default=1.0)
+    ap.add_argument("--gap", type=float, default=0.1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--eval-seeds", type=int, default=2)
+    ap.add_argument("--eval-steps", type=int, default=120)
+    ap.add_argument("--out", default="model.npz")
+    args = ap.parse_args()
+    import torch
+    device = "cuda" if torch.cuda.is_available() else "cpu"
+    cfg, _, _ = beach(1)
+    pairs = capture(range(1, args.seeds + 1), args.pairs, args.t0, args.gap)
+    weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device)
+    np.savez(args.out, **{f"w{l}": w for l, w in enumerate(weights)}, **{f"b{l}": b for l, b in enumerate(biases)},
+             input_scale=np.array(iscale, np.float32), output_scale=np.float32(oscale),
+             pairs=len(pairs), seeds=args.seeds, unexplained=unexplained)
+    print(json.dumps({"pairs": len(pairs), "unexplained_variance": unexplained, "input_scale": iscale,
+                      "output_scale": oscale, "out": args.out}), flush=True)
+    if args.eval_seeds > 0:
+        evaluate(args.out, range(101, 101 + args.eval_seeds), args.eval_steps)
+
+
+if __name__ == "__main__":
+    main()
