@@ -228,7 +228,7 @@ def ncu_traffic():
 def roofline(probes):
     """HBM roofline of the kernel with the largest probed time in one trial: algorithmic bytes per
     launch / CUDA-event time per launch, against the measured copy bandwidth."""
-    live = [p for p in probes if p["launches"] > 0 and p["ms"] > 0]
+    live = [p for p in probes if p["launches"] > 0 and p["ms"] > 0 and p["kernel"] != "all"]
     if not live:
         return None, []
     peak, source = measured_peaks()
@@ -334,6 +334,12 @@ def main():
     roof, kernels = roofline(res["probes"])
     line["roofline"] = roof
     line["probed_kernels"] = kernels
+    every = [p for p in res["probes"] if p["kernel"] == "all"]
+    if every and res["trials"]:
+        # in-situ kernel time of one trial (all launches, back to back) against the graph's time
+        line["kernel_ms_per_trial"] = every[0]["ms"]
+        line["kernel_launches_per_trial"] = every[0]["launches"]
+        line["graph_ms_per_trial"] = (res["motion_ms"] + res["pressure_ms"]) / res["trials"]
     if res["e2e"]:
         e = res["e2e"]
         line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

@@ -27,7 +27,8 @@ waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size
  * no-op): per kind, the launches, their summed CUDA-event time on the handle's stream and their
  * summed algorithmic bytes (distinct inputs read once, outputs written once).  Kinds: 0 MacCormack
  * passes, 1 level-0 Chebyshev sweeps, 2 level >= 1 sweeps (product-parallel rows), 3 level >= 1
- * sweeps (one thread per row), 4 VOF flux + update.  The trial advances the simulation like any
+ * sweeps (one thread per row), 4 VOF flux + update, 5 every kernel of the trial (launches and
+ * time only).  The trial advances the simulation like any
  * other; *trials is 0 when no trial was active (quota met). */
 typedef struct waves_kernel_probe {
   int32_t kind;

@@ -163,11 +163,19 @@ struct Grid {
     if (D.px) q.x = pidx(q.x, D.nx);
     return q;
   }
+  // d - round(d / n) * n on the periodic axes (coupled_motion.glslinc periodic_delta).  For the
+  // integer differences here (|d| <= n) round(d / n) is -1, 0 or 1, and |d / n| >= 1/2 exactly
+  // when |2d| >= n: the float quotient of two small integers never rounds onto 1/2.  So the
+  // shift is decided in integers and the result is the same float.
   DI F3 periodic_delta(I3 a, I3 b) const {
-    F3 d = mf((float)(a.x - b.x), (float)(a.y - b.y), (float)(a.z - b.z));
-    d.z -= roundf(d.z / (float)D.nz) * (float)D.nz;
-    if (D.px) d.x -= roundf(d.x / (float)D.nx) * (float)D.nx;
-    return mf(d.x * D.hx, d.y * D.hy, d.z * D.hz);
+    int dx = a.x - b.x, dz = a.z - b.z;
+    if (2 * dz >= D.nz) dz -= D.nz;
+    else if (2 * dz <= -D.nz) dz += D.nz;
+    if (D.px) {
+      if (2 * dx >= D.nx) dx -= D.nx;
+      else if (2 * dx <= -D.nx) dx += D.nx;
+    }
+    return mf((float)dx * D.hx, (float)(a.y - b.y) * D.hy, (float)dz * D.hz);
   }
 };
 
@@ -409,20 +417,47 @@ struct MaxD { DI double operator()(double a, double b) const { return a < b ? b 
 struct MinF { DI float operator()(float a, float b) const { return (b < a) ? b : a; } };
 struct MaxF { DI float operator()(float a, float b) const { return (a < b) ? b : a; } };
 
+// K values per thread reduced over the block in FP64 with few FP64 instructions: every thread
+// stores its values (one barrier), then warp w reduces value k = w, w + NT/32, ...: lane j
+// combines entries j, j + 32, j + 64, ... in that order, then a shuffle tree over the lanes.
+// The order is fixed, so the result is deterministic.  Totals land in tot[] (all threads).
+template <int NT, int K>
+DI void block_reduce_k(const double (&vals)[K], const int (&ops)[K], double* sh, double* tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) sh[k * NT + threadIdx.x] = vals[k];
+  __syncthreads();
+  for (int k = warp; k < K; k += NT / 32) {
+    const bool mx = ops[k] != 0;
+    double acc = sh[k * NT + lane];
+#pragma unroll
+    for (int i = 1; i < NT / 32; i++) {
+      const double v = sh[k * NT + lane + 32 * i];
+      acc = mx ? (acc < v ? v : acc) : acc + v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v = __shfl_down_sync(0xffffffffu, acc, o);
+      acc = mx ? (acc < v ? v : acc) : acc + v;
+    }
+    if (lane == 0) tot[k] = acc;
+  }
+  __syncthreads();
+}
+
 // Write `K` per-block partials (double), then let the last block to finish reduce all partials
 // in a fixed order.  Returns true in every thread of the last block, with the totals in `out`.
 // `ops[k]` selects 0 = sum, 1 = max for each component.
 template <int NT, int K>
 DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (&ops)[K], double (&out)[K]) {
-  __shared__ double sh[32];
+  __shared__ double sh[K * NT];
+  __shared__ double tot[K];
   __shared__ bool am_last;
   const int nb = gridDim.x * gridDim.y * gridDim.z;
   const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   double* part = D.part;
-  for (int k = 0; k < K; k++) {
-    double r = ops[k] == 0 ? block_reduce<NT>(vals[k], AddD(), sh) : block_reduce<NT>(vals[k], MaxD(), sh);
-    if (threadIdx.x == 0) part[(size_t)k * nb + bid] = r;
-  }
+  block_reduce_k<NT, K>(vals, ops, sh, tot);
+  if (threadIdx.x < K) part[(size_t)threadIdx.x * nb + bid] = tot[threadIdx.x];
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -432,14 +467,18 @@ DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (
   __syncthreads();
   if (!am_last) return false;
   __threadfence();
+  double acc[K];
+#pragma unroll
   for (int k = 0; k < K; k++) {
-    double acc = ops[k] == 0 ? 0.0 : -1e300;
+    acc[k] = ops[k] == 0 ? 0.0 : -1e300;
     for (int b = threadIdx.x; b < nb; b += NT) {
       double p = __ldcg(&part[(size_t)k * nb + b]);
-      acc = ops[k] == 0 ? acc + p : (acc < p ? p : acc);
+      acc[k] = ops[k] == 0 ? acc[k] + p : (acc[k] < p ? p : acc[k]);
     }
-    out[k] = ops[k] == 0 ? block_reduce<NT>(acc, AddD(), sh) : block_reduce<NT>(acc, MaxD(), sh);
   }
+  block_reduce_k<NT, K>(acc, ops, sh, tot);
+#pragma unroll
+  for (int k = 0; k < K; k++) out[k] = tot[k];
   if (threadIdx.x == 0) D.count[site] = 0;
   return true;
 }

@@ -110,6 +110,7 @@ struct Dev {
   const signed char* solid_tab;
   const signed char* clear_tab;  // 1 when no solid cell lies in the 3x3 (x, y) window
   const unsigned char* mac_class;  // per (axis, y, x) face column: 1 near a solid cell or the domain edge
+  unsigned char* ext_nb;         // per face: wall bit and usable extension neighbours (static)
   int* mac_list;                 // MacCormack work list (faces)
   unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
   int mac_grid;                  // persistent MacCormack blocks
@@ -147,6 +148,8 @@ struct Dev {
   int* mgcol;                // ELL columns of levels >= 1, same layout as mgell
   int mg_bottom;             // first level solved by the single-block bottom kernel
   int mg_rows_below;         // levels with fewer rows use the product-parallel apply
+  int* mg_rowlist;           // active rows of each level >= 1 (level l at lv[l].off)
+  unsigned* mg_rowcount;     // [kMaxLevels] entries of each list
   int mg_bottom_smem;        // bytes of the shared-memory bottom stage (0: bottom levels too large)
 };
 

@@ -348,6 +348,24 @@ __global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) 
   I3 l = ax(q, axis, -1);
   D.src0[f] = (!g.wall_face(q, axis) && (g.wet(q) || g.wet(l))) ? pack_face(q) : -1;
 }
+// Static neighbourhood of every face for the extension hops: bit 6 set for a wall face, bit
+// 2a + (sign > 0) set when the neighbour along axis a is in bounds and not a wall face.
+__global__ void __launch_bounds__(NT) k_ext_masks(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  Grid g(D);
+  long long f = (long long)blockIdx.x * NT + threadIdx.x;
+  if (f >= D.NF) return;
+  I3 q;
+  int axis;
+  g.unpack_face(f, q, axis);
+  unsigned bits = g.wall_face(q, axis) ? 64u : 0u;
+  for (int a = 0; a < 3; a++)
+    for (int sign = -1; sign <= 1; sign += 2) {
+      I3 nb = g.wrap_face(ax(q, a, sign));
+      if (g.face_in_bounds(nb, axis) && !g.wall_face(nb, axis)) bits |= 1u << (2 * a + (sign > 0));
+    }
+  D.ext_nb[f] = (unsigned char)bits;
+}
 __global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, int rb) {
   grid_dep_wait();
   if (!post_on(D)) return;
@@ -361,15 +379,16 @@ __global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, 
   g.unpack_face(f, q, axis);
   int source = in[f];
   float best = 1e20f;
-  if (!g.wall_face(q, axis)) {
+  const unsigned bits = D.ext_nb[f];
+  if (!(bits & 64u)) {
     if (source >= 0) {
       F3 dl = g.periodic_delta(q, unpack_coords(source));
       best = dot3(dl, dl);
     }
     for (int a = 0; a < 3; a++)
       for (int sign = -1; sign <= 1; sign += 2) {
+        if (!(bits & (1u << (2 * a + (sign > 0))))) continue;
         I3 nb = g.wrap_face(ax(q, a, sign));
-        if (!g.face_in_bounds(nb, axis) || g.wall_face(nb, axis)) continue;
         int cs = in[g.face_local(nb, axis)];
         if (cs < 0) continue;
         F3 delta = g.periodic_delta(q, unpack_coords(cs));
@@ -721,6 +740,7 @@ void launch_post(const Dev& D, cudaStream_t s) {
   pdl_launch(k_ext_write, grid_for(D.NF > D.N ? D.NF : D.N), NT, 0, s, D);
   pdl_launch(k_accept, grid_for(D.N), NT, 0, s, D);
 }
+void launch_ext_masks(const Dev& D, cudaStream_t s) { pdl_launch(k_ext_masks, grid_for(D.NF), NT, 0, s, D); }
 void launch_trial_end(const Dev& D, cudaStream_t s) { pdl_launch(k_trial_end, 1, NT, 0, s, D); }
 void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds) {
   pdl_launch(k_export, grid_for(D.N), NT, 0, s, D, planes, kinds);

@@ -333,6 +333,30 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_
   unsigned r = block_reduce<NT>(changed, AddU(), sh);
   if (threadIdx.x == 0 && r) atomicAdd(&D.hstate[20 + l], r);
 }
+// Active rows of each level >= 1, rebuilt from the current masks at every multigrid build.  The
+// sweeps, residuals and prolongations of levels >= 1 visit only these rows: an inactive row's
+// entries against active rows are exactly zero, restriction reads active children only and
+// prolongation adds at active cells only, so the rows skipped never reach level 0 (their
+// iterates stay at the zero the restriction writes).  Warps append contiguously.
+__global__ void k_mg_rows_reset(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  if (!build_on(D)) return;
+  if (threadIdx.x < kMaxLevels) D.mg_rowcount[threadIdx.x] = 0u;
+}
+template <class T> __global__ void __launch_bounds__(NT) k_mg_rowlist(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait();
+  if (!build_on(D)) return;
+  MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  const int i = blockIdx.x * NT + threadIdx.x;
+  const bool act = i < lv.count && m.active<T>(l, i);
+  const unsigned ballot = __ballot_sync(0xffffffffu, act);
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0 && ballot) base = atomicAdd(&D.mg_rowcount[l], (unsigned)__popc(ballot));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (act) D.mg_rowlist[lv.off + base + __popc(ballot & ((1u << lane) - 1u))] = i;
+}
 template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __grid_constant__ Dev D, int l) {
   grid_dep_wait();
   if (!build_on(D) || !(D.hstate[14] == 0 || D.hstate[20 + l + 1] != 0)) return;
@@ -540,13 +564,13 @@ template <class T, class M> DI void residual_cell(const M& m, int l, int f, int 
 // then one thread per row adds its products in stencil order k = 0, 1, ... -- the same roundings
 // and the same order as apply(), so the value is bit-identical.
 constexpr int RR = 32;
-template <class T> DI void row_products(const MG& m, int l, int src, int row0, float* prod, bool* inner, int* lin) {
+template <class T> DI void row_products(const MG& m, int l, int src, const int* rowi, float* prod, bool* inner, int* lin) {
   const Dev& D = m.D;
   const MGLevelDev& lv = D.lv[l];
   const int S = lv.stencil, n = lv.count;
   if (threadIdx.x < RR) {
-    int i = row0 + threadIdx.x;
-    I3 q = m.coord(l, i < n ? i : 0);
+    int i = rowi[threadIdx.x];
+    I3 q = m.coord(l, i >= 0 ? i : 0);
     inner[threadIdx.x] = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
   }
   for (int k = threadIdx.x; k < S; k += NT) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
@@ -556,9 +580,9 @@ template <class T> DI void row_products(const MG& m, int l, int src, int row0, f
   const int* col = D.mgcol + lv.eoff;
 #pragma unroll 4
   for (int p = threadIdx.x; p < S * RR; p += NT) {
-    const int k = p / RR, r = p % RR, i = row0 + r;
+    const int k = p / RR, r = p % RR, i = rowi[r];
     float v = 0.f;
-    if (i < n) {
+    if (i >= 0) {
       const long long e = (long long)k * n + i;
       const int j = inner[r] ? i + lin[k] : __ldg(col + e);
       v = ld_val(ell[e]) * ld_val(x[j]);
@@ -780,7 +804,11 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_cons
     lin_s = lin;
   }
   int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+  if (l >= 1 && op != 3) {  // sweeps, residual, prolongation: active rows only
+    if (i >= (int)D.mg_rowcount[l]) return;
+    i = D.mg_rowlist[D.lv[l].off + i];
+  } else if (i >= D.lv[l].count)
+    return;
   MG m(D);
   switch (op) {
     case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : m.apply<T>(l, a, i, lin_s)); break;
@@ -799,13 +827,17 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid
   __shared__ float prod[kMaxStencil * RR];
   __shared__ bool inner[RR];
   __shared__ int lin[kMaxStencil];
+  __shared__ int rowi[RR];
+  const int row0 = blockIdx.x * RR, nrows = (int)D.mg_rowcount[l];
+  if (row0 >= nrows) return;  // uniform over the block
   MG m(D);
-  const int row0 = blockIdx.x * RR;
+  if (threadIdx.x < RR) rowi[threadIdx.x] = row0 + threadIdx.x < nrows ? D.mg_rowlist[D.lv[l].off + row0 + threadIdx.x] : -1;
+  __syncthreads();
   const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);
-  if (need) row_products<T>(m, l, a, row0, prod, inner, lin);
+  if (need) row_products<T>(m, l, a, rowi, prod, inner, lin);
   if (threadIdx.x >= RR) return;
-  const int i = row0 + threadIdx.x;
-  if (i >= D.lv[l].count) return;
+  const int i = rowi[threadIdx.x];
+  if (i < 0) return;
   const float ax = need ? row_sum<T>(m, l, a, i, prod) : 0.f;
   switch (op) {
     case 0: cheb_update<T>(m, l, a, b, i, c != 0, ax); break;
@@ -1078,6 +1110,8 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
   pdl_launch(k_hs_decide, 1, 1, 0, s, D);
   pdl_launch((k_hs_snapshot<T>), grid_for(D.N), NT, 0, s, D);
   for (int l = 0; l < D.L; l++) pdl_launch((k_mg_mask<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+  pdl_launch(k_mg_rows_reset, 1, 32, 0, s, D);
+  for (int l = 1; l < D.L; l++) pdl_launch((k_mg_rowlist<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   pdl_launch((k_mg_nb0<T>), grid_for(D.N), NT, 0, s, D);
   for (int l = 0; l + 1 < D.L; l++) pdl_launch((k_mg_transfer<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   pdl_launch((k_mg_scale<T>), grid_for(D.lv[0].count), NT, 0, s, D, 0);

@@ -10,26 +10,6 @@ namespace wg {
 
 enum CondKind { kCondActive = 0, kCondSolving = 1, kCondDefect = 2, kCondDefectFirst = 3 };
 
-// Programmatic dependent launch: a kernel launched this way may be scheduled while the previous
-// kernel on the stream drains; every kernel's first statement is grid_dep_wait()
-// (griddepcontrol.wait), which returns once that kernel has completed and its writes are visible,
-// so only launch latency overlaps.  On by default; WAVES_PDL=0 at handle creation turns it off.
-extern bool g_pdl;
-template <class... KArgs, class... Args>
-void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cfg.attrs = attr;
-  cfg.numAttrs = g_pdl ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
-}
-
 // Kernel probes.  While a probe list is installed on the calling thread (host-scheduled trials
 // only, never during graph capture), each probed launch site brackets its launch with two events
 // on its stream and records the launch's algorithmic bytes: the distinct input arrays read once
@@ -40,7 +20,8 @@ enum ProbeKind {
   kProbeRows = 2,       // k_mgl_rows, level >= 1 sweeps with the product-parallel apply
   kProbeRowThread = 3,  // k_mgl ops 0-2, level >= 1 sweeps with one thread per row
   kProbeSweepVof = 4,   // k_sweep_update, VOF flux + update of one direction
-  kProbeCount = 5
+  kProbeAll = 5,        // every kernel of the trial (bytes not counted)
+  kProbeCount = 6
 };
 struct ProbeRec {
   int kind;
@@ -61,6 +42,27 @@ template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launc
   launch();
   cudaEventRecord(r.b, s);
   p->push_back(r);
+}
+
+// Programmatic dependent launch: a kernel launched this way may be scheduled while the previous
+// kernel on the stream drains; every kernel's first statement is grid_dep_wait()
+// (griddepcontrol.wait), which returns once that kernel has completed and its writes are visible,
+// so only launch latency overlaps.  On by default; WAVES_PDL=0 at handle creation turns it off.
+// With a probe list installed, every launch is also bracketed as kind kProbeAll.
+extern bool g_pdl;
+template <class... KArgs, class... Args>
+void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  probed(kProbeAll, s, 0.0, [&] { cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...); });
 }
 
 // k_pcg.cu
@@ -87,6 +89,7 @@ void launch_geometry(const Dev& D, cudaStream_t s);
 void launch_proj_setup(const Dev& D, cudaStream_t s);
 void launch_post(const Dev& D, cudaStream_t s);
 void launch_trial_end(const Dev& D, cudaStream_t s);
+void launch_ext_masks(const Dev& D, cudaStream_t s);  // static face neighbourhoods (set-up)
 void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds);
 // k_mg.cu
 void launch_mg_build(const Dev& D, cudaStream_t s);

@@ -360,6 +360,7 @@ waves_status setup_device(waves_handle* h) {
     AL(D.net_act, (size_t)2 * N * 16, false, "net_activations");
     AL(D.net_p, N, false, "net_pressure");
   }
+  AL(D.ext_nb, NF, false, "ext_neighbours");
   AL(D.mac_list, NF, false, "mac_list");
   AL(D.mac_ctr, 4, false, "mac_counters");
   D.mac_grid = wg::mac_blocks();
@@ -481,6 +482,8 @@ waves_status setup_device(waves_handle* h) {
     CK(cudaStreamSynchronize(h->stream));
   }
   AL(D.mgnb0, N, true, "mg_level0_neighbours");
+  AL(D.mg_rowlist, nodes, false, "mg_active_rows");
+  AL(D.mg_rowcount, wg::kMaxLevels, false, "mg_active_counts");
   AL(D.mgcol, eoff, false, "mg_ell_columns");
   // Levels from mg_bottom down run inside one thread block (latency-bound sizes).
   D.mg_bottom = D.L - 1;
@@ -813,6 +816,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
   }
   if ((st = setup_device(h)) != WAVES_OK) return fail(st);
   wg::launch_mg_cols(h->D, h->stream);
+  wg::launch_ext_masks(h->D, h->stream);
   wg::launch_initial(h->D, h->stream, h->probes);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     h->err = "initial commands failed";

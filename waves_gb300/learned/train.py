@@ -11,9 +11,12 @@ set-up b, and at the first round's convergence (relative residual 1e-6) p*.
 
 Training (PyTorch, offline): the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
 ReLU, zero padding) maps (F, b * s_b, p_prev * s_p) to (p* - p_prev) / s_out on wet cells, with
-s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data; masked
-mean squared error on random 40x32x32 crops, scored away from the crop edge (the network's
-receptive field is 4 cells).  Export: BF16 weights [co][kz][ky][kx][ci], FP32 biases, the scales.
+s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data.  The
+default objective is the initial residual the solver will see, |r0 - A (s_out y)|^2 / |r0|^2 over
+wet cells with r0 = b - A p_prev and A the ghost-fluid operator of operator_at (the residual guard
+of the solver compares exactly this norm); --objective mse fits (p* - p_prev) / s_out instead.
+Both are scored on random 40x32x32 crops away from the crop edge (the receptive field is 4 cells).
+Export: BF16 weights [co][kz][ky][kx][ci], FP32 biases, the scales.
 
 Evaluation: held-out seeds run the same number of steps with and without the network; the
 result line gives CG iterations and pressure milliseconds per step for both.
@@ -30,6 +33,7 @@ import waves_gb300 as wg
 from waves_gb300.learned import CHANNELS, bf16_bits, load_model
 
 DEPTH = 0.45
+WITH_COEF = True  # capture the ghost-fluid face coefficients (needed by the residual objective)
 
 
 def beach(seed, warm=0):
@@ -55,6 +59,7 @@ def capture_trial(s, N, NF):
     bank = s.bank(cand)
     F, p_prev = bank[:N].copy(), bank[N + NF:N + NF + N].copy()
     kind = s.geometry()[1].copy()
+    coef = s.debug_read("coef", 6 * N) if WITH_COEF else None
     s.debug_phase(7)
     pair, rounds = None, 0
     while True:
@@ -66,7 +71,7 @@ def capture_trial(s, N, NF):
             c = s.control()
         if rounds == 0 and c[6] > 0.5 and c[7] < 0.5:
             p_star = s.bank(cand)[N + NF:N + NF + N].copy()
-            pair = {"F": F, "b": b, "p_prev": p_prev, "p_star": p_star, "kind": kind}
+            pair = {"F": F, "b": b, "p_prev": p_prev, "p_star": p_star, "kind": kind, "coef": coef}
         s.debug_phase(10)
         c = s.control()
         rounds += 1
@@ -105,7 +110,27 @@ def build_net(torch):
     return torch.nn.Sequential(*layers)
 
 
-def train(pairs, n, steps, seed, device):
+def apply_operator(torch, x, coef, wet, periodic_x=False):
+    """operator_at (pressure_core.glslinc:98-104) on [B, 1, z, y, x] fields: sum over the six faces
+    of coef_f * (x_here - x_neighbour), neighbours outside or dry contributing zero, z periodic."""
+    xw = x * wet
+    out = torch.zeros_like(x)
+    for f, (dim, sign) in enumerate(((4, -1), (4, 1), (3, -1), (3, 1), (2, -1), (2, 1))):
+        if dim == 2 or (dim == 4 and periodic_x):
+            other = torch.roll(xw, shifts=-sign, dims=dim)
+        else:
+            pad = [0, 0, 0, 0, 0, 0]
+            k = 2 * (4 - dim) + (1 if sign > 0 else 0)  # pad the far side of the shifted axis
+            pad[k] = 1
+            other = torch.nn.functional.pad(xw, pad)
+            idx = [slice(None)] * 5
+            idx[dim] = slice(1, None) if sign > 0 else slice(0, -1)
+            other = other[tuple(idx)]
+        out = out + coef[:, f:f + 1] * (xw - other)
+    return out * wet
+
+
+def train(pairs, n, steps, seed, device, objective="residual"):
     import torch
     torch.manual_seed(seed)
     nx, ny, nz = n
@@ -121,6 +146,10 @@ def train(pairs, n, steps, seed, device):
     x = torch.stack([F, b * s_b, pp * s_p], dim=1)
     y = (dp / s_out)[:, None]
     m = wet[:, None].float()
+    if objective == "residual":
+        coef = torch.stack([torch.from_numpy(p["coef"].reshape(6, nz, ny, nx)).to(device) for p in pairs]).float()
+        r0 = torch.stack([grid(p["b"]) for p in pairs])[:, None] * m - apply_operator(torch, pp[:, None], coef, m)
+        s_r = max(float(r0[m > 0].std()), 1e-12)
     net = build_net(torch).to(device)
     opt = torch.optim.Adam(net.parameters(), lr=2e-3)
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
@@ -137,16 +166,27 @@ def train(pairs, n, steps, seed, device):
         ms = torch.stack([m[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
         e = (slice(None), slice(None), slice(edge, cz - edge), slice(edge, cy - edge), slice(edge, cx - edge))
         pred = net(xs)
-        loss = ((pred - ys)[e] ** 2 * ms[e]).sum() / ms[e].sum().clamp(min=1.0)
+        if objective == "residual":
+            cs = torch.stack([coef[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
+            rs = torch.stack([r0[i, :, z:z + cz, yy:yy + cy, xx:xx + cx] for i, xx, yy, z in zip(idx, ox, oy, oz)])
+            res = (rs - apply_operator(torch, pred * s_out, cs, ms)) / s_r
+            loss = (res[e] ** 2 * ms[e]).sum() / ms[e].sum().clamp(min=1.0)
+        else:
+            loss = ((pred - ys)[e] ** 2 * ms[e]).sum() / ms[e].sum().clamp(min=1.0)
         opt.zero_grad()
         loss.backward()
         opt.step()
         sched.step()
         if step % max(steps // 10, 1) == 0 or step == steps - 1:
             print(f"step {step}: masked MSE {loss.item():.4e} ({time.time() - t0:.1f} s)", flush=True)
-    with torch.no_grad():  # whole-field fit on the training pairs (fraction of variance left)
-        resid = sum(float((((net(x[i:i + 1]) - y[i:i + 1]) ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
-        total = sum(float(((y[i:i + 1] ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
+    with torch.no_grad():  # whole-field score on the training pairs: fraction of the objective left
+        if objective == "residual":
+            resid = sum(float((((r0[i:i + 1] - apply_operator(torch, net(x[i:i + 1]) * s_out, coef[i:i + 1], m[i:i + 1])) ** 2)
+                               * m[i:i + 1]).sum()) for i in range(len(pairs)))
+            total = sum(float(((r0[i:i + 1] ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
+        else:
+            resid = sum(float((((net(x[i:i + 1]) - y[i:i + 1]) ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
+            total = sum(float(((y[i:i + 1] ** 2) * m[i:i + 1]).sum()) for i in range(len(pairs)))
     convs = [mod for mod in net if isinstance(mod, torch.nn.Conv3d)]
     weights = [bf16_bits(c.weight.detach().permute(0, 2, 3, 4, 1).contiguous().cpu().numpy()) for c in convs]
     biases = [c.bias.detach().cpu().numpy().astype(np.float32) for c in convs]
@@ -192,16 +232,17 @@ def main():
     ap.add_argument("--eval-seeds", type=int, default=2)
     ap.add_argument("--eval-steps", type=int, default=120)
     ap.add_argument("--out", default="model.npz")
+    ap.add_argument("--objective", default="residual", choices=["residual", "mse"])
     args = ap.parse_args()
     import torch
     device = "cuda" if torch.cuda.is_available() else "cpu"
     cfg, _, _ = beach(1)
     pairs = capture(range(1, args.seeds + 1), args.pairs, args.t0, args.gap)
-    weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device)
+    weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device, args.objective)
     np.savez(args.out, **{f"w{l}": w for l, w in enumerate(weights)}, **{f"b{l}": b for l, b in enumerate(biases)},
              input_scale=np.array(iscale, np.float32), output_scale=np.float32(oscale),
              pairs=len(pairs), seeds=args.seeds, unexplained=unexplained)
-    print(json.dumps({"pairs": len(pairs), "unexplained_variance": unexplained, "input_scale": iscale,
+    print(json.dumps({"pairs": len(pairs), "objective": args.objective, "fraction_left": unexplained, "input_scale": iscale,
                       "output_scale": oscale, "out": args.out}), flush=True)
     if args.eval_seeds > 0:
         evaluate(args.out, range(101, 101 + args.eval_seeds), args.eval_steps)
