@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mg", type=int, default=32, choices=[32, 16])
+    ap.add_argument("--grid", default="beach", choices=["beach", "large"],
+                    help="beach: 310x48x80 (the metric's grid); large: 620x96x160, spacing halved")
     ap.add_argument("--e2e-frames", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -97,9 +99,12 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def beach_config(mg):
+GRIDS = {"beach": {}, "large": {"n": (620, 96, 160), "spacing": (0.0125, 0.0125, 0.025)}}
+
+
+def beach_config(mg, grid="beach"):
     import waves_gb300 as wg
-    return wg.config("beach", pressure_tolerance=TOL, mg_precision=mg)
+    return wg.config("beach", pressure_tolerance=TOL, mg_precision=mg, **GRIDS[grid])
 
 
 def run_ours(args, world, rank, local):
@@ -111,7 +116,7 @@ def run_ours(args, world, rank, local):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.set_device(local)
-    cfg = beach_config(args.mg)
+    cfg = beach_config(args.mg, args.grid)
     cfg.device = local
     s = wg.WavesSolver(cfg)
     lib, h = s.lib, s.h
@@ -290,16 +295,10 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
     res = run_ours(args, world, rank, local)
     sim, dev = res["sim_s"], res["device_s"]
-    if world > 1:
-        t = torch.tensor([sim, dev, res["e2e"]["sim_s"] if res["e2e"] else 0.0], dtype=torch.float64, device=f"cuda:{local}")
-        mx = torch.tensor([dev, res["e2e"]["wall_s"] if res["e2e"] else 0.0], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sim_total, dev_max, e2e_sim, e2e_wall = t[0].item(), mx[0].item(), t[2].item(), mx[1].item()
-    else:
-        sim_total, dev_max = sim, dev
-        e2e_sim = res["e2e"]["sim_s"] if res["e2e"] else 0.0
-        e2e_wall = res["e2e"]["wall_s"] if res["e2e"] else 0.0
+    from waves_gb300.replicas import aggregate
+    e = res["e2e"] or {"sim_s": 0.0, "wall_s": 0.0}
+    sim_total, dev_max, e2e_sim, e2e_wall = aggregate(sim, dev, e["sim_s"], e["wall_s"],
+                                                      device=f"cuda:{local}" if world > 1 else None)
     if rank != 0:
         torch.distributed.destroy_process_group() if world > 1 else None
         return
@@ -317,9 +316,10 @@ def main():
         "vs_baseline": None,
         "dtype": "f32" if args.mg == 32 else "f32+bf16mg",
         "data": "synthetic",
-        "config": {"workload": "beach 310x48x80 (lab_runner.gd settings), "
+        "config": {"workload": ("beach 310x48x80 (lab_runner.gd settings), " if args.grid == "beach" else
+                                "beach 620x96x160 (lab_runner.gd settings, spacing halved), ")
                                + ("plain FP32 MGPCG" if args.mg == 32 else "BF16 multigrid, FP32 CG") + ", tol 1e-6",
-                   "cells": 1190400, "l2": "flushed between steps (256 MiB write)",
+                   "cells": 1190400 if args.grid == "beach" else 9523200, "l2": "flushed between steps (256 MiB write)",
                    "sim_window_s": [res["t_end"] - res["sim_s"], res["t_end"]],
                    "parallelism": "replicas" if world > 1 else "single"},
         "pressure_ms_per_step": res["pressure_ms"] / steps,

@@ -46,3 +46,17 @@ def test_create_without_device_fails_cleanly(monkeypatch):
     import pytest
     with pytest.raises(waves_gb300.WavesError):
         waves_gb300.WavesSolver(waves_gb300.config("tank"))
+
+
+def test_harness_argument_and_device_errors():
+    """The C harness (built by build()) exits 1 on a bad argument and 2, with the library's
+    message, when there is no usable device."""
+    import subprocess
+    from waves_gb300.build import HARNESS, build
+    build()
+    r = subprocess.run([HARNESS, "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 1 and "usage" in r.stderr
+    import torch
+    if not torch.cuda.is_available():
+        r = subprocess.run([HARNESS, "--preset", "tank", "--steps", "1"], capture_output=True, text=True)
+        assert r.returncode == 2 and "waves_create" in r.stderr

@@ -72,11 +72,12 @@ def test_step_parity(gpu_lib, name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["beach_slope", "beach_slope_bf16"])
-@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1"])
+@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1", "WAVES_MG_COARSE=1"])
 def test_step_parity_kernel_variants(gpu_lib, name, variant, monkeypatch):
     """Kernel forms that the small grids above do not reach: the level >= 1 sweeps with one
-    thread per row (large levels use it; small ones use the product-parallel rows), and the
-    bottom levels solved from global memory (used when they do not fit the shared-memory stage)."""
+    thread per row (large levels use it; small ones use the product-parallel rows), the bottom
+    levels solved from global memory (used when they do not fit the shared-memory stage), and the
+    coarse levels as one cooperative launch instead of level by level."""
     key, value = variant.split("=")
     monkeypatch.setenv(key, value)
     cfg = CASES[name]()
@@ -89,3 +90,49 @@ def test_step_parity_kernel_variants(gpu_lib, name, variant, monkeypatch):
         o.run()
         problems = compare_state(g, o, cfg, f"step {step}")
         assert not problems, "\n".join(problems)
+
+
+@pytest.mark.gpu
+def test_injected_rejection_parity(gpu_lib):
+    """Host-side fault injection: c19 (waves_inject_rejection) forces code 4 at the next
+    acceptance (pressure_pass.glslinc:268); the GPU rolls back and halts exactly as the oracle."""
+    cfg = CASES["tank_small"]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    g.request_steps(1)
+    g.run()
+    o.request_steps(1)
+    o.run()
+    g.inject_rejection()
+    c = o.control()
+    c[19] = 1
+    o.set_control(c)
+    g.request_steps(2)
+    assert g.run() == 4  # WAVES_SOLVER_FAILED
+    o.request_steps(2)
+    o.run()
+    cg = g.control()
+    assert cg[7] == 4 and cg[3] == 1 and cg[2] == 1 and g.stats()["failure"] == 4
+    problems = compare_state(g, o, cfg, "after injected rejection")
+    assert not problems, "\n".join(problems)
+
+
+@pytest.mark.gpu
+def test_poisoned_fraction_retry_parity(gpu_lib):
+    """A volume fraction of 1.5 fails the sweep bound (codes 10-12), the trial is rolled back and
+    retried at half dt (coupled_motion.glslinc:351-355), on the GPU exactly as on the oracle."""
+    cfg = CASES["tank_small"]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for s in (g, o):
+        b = s.bank(0)
+        b[5] = 1.5
+        s.set_bank(0, b)
+    g.request_steps(1)
+    g.run()
+    o.request_steps(1)
+    o.run()
+    cg, co = g.control(), o.control()
+    assert cg[33] in (10.0, 11.0, 12.0) or cg[7] in (10.0, 11.0, 12.0)
+    problems = compare_state(g, o, cfg, "after poisoned fraction")
+    assert not problems, "\n".join(problems)

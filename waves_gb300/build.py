@@ -42,7 +42,10 @@ def _stale(objs):
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "waves.h")]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "waves.h"),
+                                                                 os.path.join(HERE, "harness", "waves_run.c")]
+    if not os.path.exists(HARNESS):
+        return True
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
@@ -62,7 +65,26 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_harness()
     return LIB
+
+
+HARNESS = os.path.join(OUT, "waves_run")
+
+
+def build_harness():
+    """The headless C driver (harness/waves_run.c), linked against the library with an rpath."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        raise RuntimeError("no C compiler for the harness")
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = [cc, "-std=c11", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"),
+           os.path.join(HERE, "harness", "waves_run.c"), "-o", HARNESS, "-L", OUT, "-lwaves_gb300",
+           "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness build failed:\n{r.stdout}\n{r.stderr}")
+    return HARNESS
 
 
 if __name__ == "__main__":

@@ -151,6 +151,9 @@ struct Dev {
   int* mg_rowlist;           // active rows of each level >= 1 (level l at lv[l].off)
   unsigned* mg_rowcount;     // [kMaxLevels] entries of each list
   int mg_bottom_smem;        // bytes of the shared-memory bottom stage (0: bottom levels too large)
+  int mg_coarse_from;        // first level of the one-launch coarse V-cycle (0: not used)
+  int coarse_blocks;         // blocks of that cooperative launch (one per SM)
+  unsigned* gbar;            // its grid barrier: arrival count, generation
 };
 
 // Reduction sites (one last-block counter each).

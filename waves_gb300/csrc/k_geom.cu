@@ -557,27 +557,31 @@ __global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D)
   const float* A = bank_ptr(D, acc_bank(D));
   double* c = D.c;
   if (D.coastal) {
-    // op 85: gauges of the accepted state
-    for (int t = threadIdx.x; t < 8 * D.nz; t += NT) {
-      int gi = t / D.nz, z = t % D.nz;
-      float begin = D.forcing[0] + D.forcing[1] + .4f;
-      float end = D.ox + (float)D.nx * D.hx - (D.shape == 6 ? D.forcing[1] + .4f : 1.0f);
-      float tt = (float)gi / 7.f;
-      float pos = begin * (1.f - tt) + end * tt;
-      int x = min(max((int)((pos - D.ox) / D.hx), 0), D.nx - 1);
-      float column = D.oy;
-      for (int y = 0; y < D.ny; y++) {
-        I3 q = mk(x, y, z);
-        column += (g.solid(q) ? 1.f : A[g.index3(q)]) * D.hy;
+    // op 85: gauges of the accepted state; the column heights of 128 z planes at a time, each
+    // gauge's sum taken in z order
+    float height = 0.f;
+    for (int z0 = 0; z0 < D.nz; z0 += 128) {
+      for (int t = threadIdx.x; t < 8 * 128; t += NT) {
+        const int gi = t / 128, z = z0 + t % 128;
+        if (z >= D.nz) continue;
+        float begin = D.forcing[0] + D.forcing[1] + .4f;
+        float end = D.ox + (float)D.nx * D.hx - (D.shape == 6 ? D.forcing[1] + .4f : 1.0f);
+        float tt = (float)gi / 7.f;
+        float pos = begin * (1.f - tt) + end * tt;
+        int x = min(max((int)((pos - D.ox) / D.hx), 0), D.nx - 1);
+        float column = D.oy;
+        for (int y = 0; y < D.ny; y++) {
+          I3 q = mk(x, y, z);
+          column += (g.solid(q) ? 1.f : A[g.index3(q)]) * D.hy;
+        }
+        cols[t] = column;
       }
-      if (z < 128) cols[gi * 128 + z] = column;
+      __syncthreads();
+      if (threadIdx.x < 8)
+        for (int z = z0; z < D.nz && z < z0 + 128; z++) height += cols[threadIdx.x * 128 + (z - z0)];
+      __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x < 8) {
-      float height = 0.f;
-      for (int z = 0; z < D.nz && z < 128; z++) height += cols[threadIdx.x * 128 + z];
-      c[80 + threadIdx.x] = (double)(height / (float)D.nz);
-    }
+    if (threadIdx.x < 8) c[80 + threadIdx.x] = (double)(height / (float)D.nz);
     __syncthreads();
   }
   if (threadIdx.x != 0) return;

@@ -564,23 +564,24 @@ template <class T, class M> DI void residual_cell(const M& m, int l, int f, int 
 // then one thread per row adds its products in stencil order k = 0, 1, ... -- the same roundings
 // and the same order as apply(), so the value is bit-identical.
 constexpr int RR = 32;
-template <class T> DI void row_products(const MG& m, int l, int src, const int* rowi, float* prod, bool* inner, int* lin) {
+template <class T, int NTB = NT, int RRB = RR>
+DI void row_products(const MG& m, int l, int src, const int* rowi, float* prod, bool* inner, int* lin) {
   const Dev& D = m.D;
   const MGLevelDev& lv = D.lv[l];
   const int S = lv.stencil, n = lv.count;
-  if (threadIdx.x < RR) {
+  if (threadIdx.x < RRB) {
     int i = rowi[threadIdx.x];
     I3 q = m.coord(l, i >= 0 ? i : 0);
     inner[threadIdx.x] = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
   }
-  for (int k = threadIdx.x; k < S; k += NT) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
+  for (int k = threadIdx.x; k < S; k += NTB) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
   __syncthreads();
   const T* x = m.field<T>(src, l);
   const T* ell = (const T*)D.mgell + lv.eoff;
   const int* col = D.mgcol + lv.eoff;
 #pragma unroll 4
-  for (int p = threadIdx.x; p < S * RR; p += NT) {
-    const int k = p / RR, r = p % RR, i = rowi[r];
+  for (int p = threadIdx.x; p < S * RRB; p += NTB) {
+    const int k = p / RRB, r = p % RRB, i = rowi[r];
     float v = 0.f;
     if (i >= 0) {
       const long long e = (long long)k * n + i;
@@ -591,11 +592,11 @@ template <class T> DI void row_products(const MG& m, int l, int src, const int* 
   }
   __syncthreads();
 }
-template <class T> DI float row_sum(const MG& m, int l, int src, int i, const float* prod) {
+template <class T, int RRB = RR> DI float row_sum(const MG& m, int l, int src, int i, const float* prod) {
   if (!m.active<T>(l, i)) return ld_val(m.field<T>(src, l)[i]);
   const int S = m.D.lv[l].stencil;
   float sum = 0.f;
-  for (int k = 0; k < S; k++) sum += prod[k * RR + threadIdx.x];
+  for (int k = 0; k < S; k++) sum += prod[k * RRB + threadIdx.x];
   return sum;
 }
 
@@ -847,29 +848,28 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid
 }
 
 // Shared-memory view of the bottom levels lb..L-1: their eight vector fields (one span per field,
-// levels in global order) and their ELL row values are staged in shared memory; columns are
-// recomputed from the stencil offsets (max(wrap(q + offset), 0), the cached columns), so apply()
-// reads the same values in the same order as the global-memory form.
+// levels in global order), their ELL row values and the cached columns max(wrap(q + offset), 0)
+// (as 16-bit indices: a bottom level holds at most 1024 rows) are staged in shared memory, so
+// apply() reads the same values in the same order as the global-memory form.
 struct MGs : MG {
   void* vec;
   const void* ell;
+  const unsigned short* cols;  // the cached columns max(wrap(q + offset), 0) of the staged rows
   int base_off, span;
   long long base_eoff;
-  DI MGs(const Dev& d, void* v, const void* e, int lb, int sp)
-      : MG(d), vec(v), ell(e), base_off(d.lv[lb].off), span(sp), base_eoff(d.lv[lb].eoff) {}
+  DI MGs(const Dev& d, void* v, const void* e, const unsigned short* c, int lb, int sp)
+      : MG(d), vec(v), ell(e), cols(c), base_off(d.lv[lb].off), span(sp), base_eoff(d.lv[lb].eoff) {}
   template <class T> DI T* field(int f, int l) const { return (T*)vec + f * span + (D.lv[l].off - base_off); }
   template <class T> DI bool active(int l, int i) const { return i >= 0 && ld_val(field<T>(3, l)[i]) > .5f; }
   template <class T> DI float apply(int l, int f, int i, const int* = nullptr) const {
     const T* x = field<T>(f, l);
     if (!active<T>(l, i)) return ld_val(x[i]);
     const MGLevelDev& lv = D.lv[l];
-    const T* e = (const T*)ell + (lv.eoff - base_eoff);
-    const I3 q = coord(l, i);
+    const long long at = lv.eoff - base_eoff;
+    const T* e = (const T*)ell + at;
+    const unsigned short* c = cols + at;
     float sum = 0.f;
-    for (int k = 0; k < lv.stencil; k++) {
-      const int j = wrap(l, addI(q, offset(l, k)));
-      sum += ld_val(e[k * lv.count + i]) * ld_val(x[j > 0 ? j : 0]);
-    }
+    for (int k = 0; k < lv.stencil; k++) sum += ld_val(e[k * lv.count + i]) * ld_val(x[c[k * lv.count + i]]);
     return sum;
   }
 };
@@ -924,27 +924,137 @@ template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __g
   bottom_cycle<T>(D, MG(D), lb, small);
 }
 // The same with levels lb..L-1 staged in shared memory (D.mg_bottom_smem bytes: 8 fields of
-// `span` values, then the ELL values, 16-byte aligned): load, cycle, write the fields back.
-template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom_smem(const __grid_constant__ Dev D, int phase, int lb) {
-  grid_dep_wait();
-  if (!phase_on(D, phase)) return;
-  extern __shared__ __align__(16) unsigned char stage[];
-  __shared__ float small[64];
+// `span` values, the ELL values and their columns as 16-bit indices, each part 16-byte aligned):
+// load, cycle, write the fields back.
+// Levels lb..L-1 staged in `stage` by one block, the sub-cycle run there, the fields written back.
+template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* stage, float* small) {
   const int L = D.L;
   const int span = D.lv[L - 1].off + D.lv[L - 1].count - D.lv[lb].off;
   const long long e0 = D.lv[lb].eoff, e1 = D.lv[L - 1].eoff + (long long)D.lv[L - 1].stencil * D.lv[L - 1].count;
   T* vec = (T*)stage;
   T* ell = (T*)(stage + (((size_t)8 * span * sizeof(T) + 15) & ~(size_t)15));
+  unsigned short* cols = (unsigned short*)((unsigned char*)ell + (((size_t)(e1 - e0) * sizeof(T) + 15) & ~(size_t)15));
   const T* gvec = (const T*)D.mgv + D.lv[lb].off;
   for (int f = 0; f < 8; f++)
     for (int k = threadIdx.x; k < span; k += blockDim.x) vec[f * span + k] = gvec[(size_t)f * D.mg_nodes + k];
   const T* gell = (const T*)D.mgell + e0;
-  for (long long k = threadIdx.x; k < e1 - e0; k += blockDim.x) ell[k] = gell[k];
+  const int* gcol = D.mgcol + e0;
+  for (long long k = threadIdx.x; k < e1 - e0; k += blockDim.x) {
+    ell[k] = gell[k];
+    cols[k] = (unsigned short)gcol[k];
+  }
   __syncthreads();
-  bottom_cycle<T>(D, MGs(D, vec, ell, lb, span), lb, small);
+  bottom_cycle<T>(D, MGs(D, vec, ell, cols, lb, span), lb, small);
   T* out = (T*)D.mgv + D.lv[lb].off;
   for (int f = 0; f < 8; f++)
     for (int k = threadIdx.x; k < span; k += blockDim.x) out[(size_t)f * D.mg_nodes + k] = vec[f * span + k];
+}
+template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom_smem(const __grid_constant__ Dev D, int phase, int lb) {
+  grid_dep_wait();
+  if (!phase_on(D, phase)) return;
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ float small[64];
+  bottom_staged<T>(D, lb, stage, small);
+}
+
+// ---------------------------------------------------------------- coarse levels in one launch
+// Levels mg_coarse_from..L-1 of a V-cycle run in one cooperative launch (one block per SM, all
+// blocks resident): every phase of Cycle::level for those levels -- Chebyshev or Jacobi sweeps and
+// residuals over the active rows (product-parallel chunks of CRR rows), restrictions, the bottom
+// sub-cycle in block 0 and prolongations -- in the same order, with the same per-row functions,
+// separated by grid barriers.  The level-from correction ends in field 1, as in Cycle.
+constexpr int CNT = 512;  // threads per block of the coarse kernel
+constexpr int CRR = 64;   // rows per product-parallel chunk
+
+// Grid barrier: arrive on a counter; the last block resets it and advances the generation the
+// others wait on.  The wait is bounded (about a second of __nanosleep): on a timeout the block
+// records failure 98 in c[7] and carries on, so no launch can hang.
+DI void grid_barrier(const Dev& D) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = D.gbar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(D.gbar, 1u) == gridDim.x - 1) {
+      D.gbar[0] = 0u;
+      __threadfence();
+      atomicAdd(D.gbar + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*gen == g) {
+        __nanosleep(128);
+        if (++spins > (1u << 23)) {
+          D.c[7] = 98;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(CNT) k_mg_coarse(const __grid_constant__ Dev D, int phase, int lt) {
+  grid_dep_wait();
+  if (!phase_on(D, phase)) return;  // the same decision in every block
+  extern __shared__ __align__(16) unsigned char dyn[];
+  __shared__ bool inner[CRR];
+  __shared__ int lin[kMaxStencil];
+  __shared__ int rowi[CRR];
+  __shared__ float small[64];
+  float* prod = (float*)dyn;
+  const MG m(D);
+  const int lb = D.mg_bottom;
+  int field[kMaxLevels];
+  auto rows_op = [&](int l, int op, int a, int b, int c) {
+    const int nrows = (int)D.mg_rowcount[l];
+    const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);
+    for (int row0 = blockIdx.x * CRR; row0 < nrows; row0 += gridDim.x * CRR) {
+      if (threadIdx.x < CRR) rowi[threadIdx.x] = row0 + threadIdx.x < nrows ? D.mg_rowlist[D.lv[l].off + row0 + threadIdx.x] : -1;
+      __syncthreads();
+      if (need) row_products<T, CNT, CRR>(m, l, a, rowi, prod, inner, lin);
+      if (threadIdx.x < CRR && rowi[threadIdx.x] >= 0) {
+        const int i = rowi[threadIdx.x];
+        const float ax = need ? row_sum<T, CRR>(m, l, a, i, prod) : 0.f;
+        if (op == 0) cheb_update<T>(m, l, a, b, i, c != 0, ax);
+        else if (op == 1) jacobi_update<T>(m, l, a, b, i, ax);
+        else residual_update<T>(m, l, i, ax);
+      }
+      __syncthreads();
+    }
+    grid_barrier(D);
+  };
+  auto smooth = [&](int l, int f, bool zero) {
+    for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
+      const bool first = zero && sweep == 0;
+      if (D.mg_smoother == 1) rows_op(l, 0, f, sweep + 1, first ? 1 : 0);
+      else rows_op(l, 1, f, first ? 1 : 0, 0);
+      f = 3 - f;
+    }
+    return f;
+  };
+  for (int l = lt; l < lb; l++) {
+    const int f = smooth(l, 1, true);
+    field[l] = f;
+    rows_op(l, 2, f, 0, 0);
+    for (int i = blockIdx.x * CNT + threadIdx.x; i < D.lv[l + 1].count; i += gridDim.x * CNT) restrict_cell<T>(m, l + 1, i);
+    grid_barrier(D);
+  }
+  if (blockIdx.x == 0) {
+    if (D.mg_bottom_smem > 0) bottom_staged<T>(D, lb, dyn, small);
+    else bottom_cycle<T>(D, m, lb, small);
+  }
+  grid_barrier(D);
+  int cf = 1;
+  for (int l = lb - 1; l >= lt; l--) {
+    const int f = field[l];
+    const int nrows = (int)D.mg_rowcount[l];
+    for (int t = blockIdx.x * CNT + threadIdx.x; t < nrows; t += gridDim.x * CNT)
+      prolong_cell<T>(m, l, f, cf, D.mg_rowlist[D.lv[l].off + t]);
+    grid_barrier(D);
+    cf = smooth(l, f, false);
+  }
 }
 
 // op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
@@ -1001,6 +1111,26 @@ double smooth0_bytes(const Dev& D, int phase, int k, int src_zero, int fin, doub
   return bytes;
 }
 
+// A cooperative launch of the coarse kernel; the grid must fit the device at once (one block
+// per SM), which the launch itself checks.
+template <class... KArgs, class... Args>
+void coop_launch(void (*kernel)(KArgs...), unsigned blocks, unsigned threads, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  probed(kProbeAll, s, 0.0, [&] { cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...); });
+}
+__global__ void k_coop_probe(int* x) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *x = 1;
+}
+
 template <class T> struct Cycle {
   const Dev& D;
   cudaStream_t s;
@@ -1046,6 +1176,13 @@ template <class T> struct Cycle {
   int bottom_field() const { return 1; }
   int level(int l) {
     unsigned gr = grid_for(D.lv[l].count);
+    if (D.mg_coarse_from > 0 && l == D.mg_coarse_from && l < D.mg_bottom) {
+      const size_t smem = std::max((size_t)kMaxStencil * CRR * sizeof(float), (size_t)D.mg_bottom_smem);
+      coop_launch((k_mg_coarse<T>), D.coarse_blocks, CNT, smem, s, D, phase, l);
+      int f = 1;  // the field logic of the kernel: pre- then post-smoothing from field 1
+      for (int k = 0; k < 2 * D.mg_smoothing; k++) f = 3 - f;
+      return f;
+    }
     if (l == D.L - 1 || l == D.mg_bottom) {
       if (D.mg_bottom_smem > 0 && l == D.mg_bottom)
         pdl_launch((k_mg_bottom_smem<T>), 1, 1024, D.mg_bottom_smem, s, D, phase, l);
@@ -1141,7 +1278,52 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
 void launch_mg_cols(const Dev& D, cudaStream_t s) {
   for (int l = 1; l < D.L; l++) pdl_launch(k_mg_cols, grid_for(D.lv[l].count), NT, 0, s, D, l);
 }
+// Blocks of the coarse launch (one per SM when the kernel fits once per SM, else 0) and whether a
+// cooperative launch can be captured into a graph on this device (checked once per call).
+int coarse_blocks(size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_coarse<float>, CNT, smem) != cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  int per_sm16 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm16, k_mg_coarse<__nv_bfloat16>, CNT, smem) != cudaSuccess || per_sm16 < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  int* x = nullptr;
+  cudaStream_t s = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t e = nullptr;
+  bool ok = cudaMalloc(&x, sizeof(int)) == cudaSuccess && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)sms);
+    cfg.blockDim = dim3(32);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const bool launched = cudaLaunchKernelEx(&cfg, k_coop_probe, x) == cudaSuccess;
+    ok = cudaStreamEndCapture(s, &g) == cudaSuccess && launched && g && cudaGraphInstantiate(&e, g, 0) == cudaSuccess &&
+         cudaGraphLaunch(e, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+  }
+  if (e) cudaGraphExecDestroy(e);
+  if (g) cudaGraphDestroy(g);
+  if (s) cudaStreamDestroy(s);
+  if (x) cudaFree(x);
+  cudaGetLastError();
+  return ok ? sms : 0;
+}
+
 void mg_kernel_attributes() {
+  cudaFuncSetAttribute(k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
+  cudaFuncSetAttribute(k_mg_coarse<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
   cudaFuncSetAttribute(k_mg_bottom_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
   cudaFuncSetAttribute(k_mg_bottom_smem<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax);
   cudaFuncSetAttribute(k_mg_galerkin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 125 * GT * (int)sizeof(float));

@@ -161,6 +161,26 @@ __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) 
   }
 }
 
+// ---------------------------------------------------------------- op 22 (faces and pressure)
+// candidate <- accepted (coupled_motion.glslinc:370-373).  The sweeps rewrite every F, so only the
+// faces and the pressure are copied; in an accepted trial MacCormack and op 2 overwrite them too,
+// but a trial that fails before them (CFL, compression, sweep bounds) leaves this copy, as the
+// reference does.  c_i is set by k_compress.
+__global__ void __launch_bounds__(NT) k_stage_candidate(const __grid_constant__ Dev D) {
+  grid_dep_wait();
+  if (!setup_on(D)) return;
+  const int acc = acc_bank(D);
+  const float4* src = reinterpret_cast<const float4*>(bank_ptr(D, acc) + D.N);
+  float4* dst = reinterpret_cast<float4*>(bank_ptr(D, 1 - acc) + D.N);
+  const long long n = D.NF + D.N, n4 = (D.N % 4 == 0 && n % 4 == 0) ? n / 4 : 0;  // 16-byte aligned, whole
+  const long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (n4) {
+    if (i < n4) dst[i] = src[i];
+  } else if (i < n) {
+    bank_ptr(D, 1 - acc)[D.N + i] = bank_ptr(D, acc)[D.N + i];
+  }
+}
+
 // ---------------------------------------------------------------- op 23
 __global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev D) {
   grid_dep_wait();
@@ -181,11 +201,13 @@ __global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev 
   D.plane[i] = out;
 }
 
-// op 24 flux of one sweep-axis face (coupled_motion.glslinc:375-388)
-DI float sweep_flux(const Motion& m, I3 q, int axis) {
+// op 24 flux of one sweep-axis face (coupled_motion.glslinc:375-388); `courant` returns the face's
+// Courant number old_face * dt / h (the face_courant expression), which the update needs as well.
+DI float sweep_flux(const Motion& m, I3 q, int axis, float& courant) {
   const Dev& D = m.D;
+  const float velocity = m.old_face(q, axis);
+  courant = velocity * m.dt / m.g.h(axis);
   if (m.g.wall_face(q, axis)) return 0.f;
-  float velocity = m.old_face(q, axis), courant = m.face_courant(q, axis);
   I3 donor = q;
   if (velocity > 0.f) donor[axis]--;
   donor = m.g.wrap_cell(donor);
@@ -214,9 +236,10 @@ __global__ void __launch_bounds__(NT) k_sweep_update(const __grid_constant__ Dev
   double v[9] = {-1e20, -1e20, 0, 0, 0, 0, 0, 0, 0};
   if (i < D.N) {
     I3 q = m.g.coord(i), r = ax(q, sa, 1);
-    float fq = sweep_flux(m, q, sa), fr_ = sweep_flux(m, r, sa);
+    float cq, cr;
+    float fq = sweep_flux(m, q, sa, cq), fr_ = sweep_flux(m, r, sa, cr);
     float net = fq - fr_;
-    float correction = D.mci[i] * (m.face_courant(r, sa) - m.face_courant(q, sa));
+    float correction = D.mci[i] * (cr - cq);
     float increment = net + correction;
     float fin = m.transport_f(q);
     float f = fin + increment;
@@ -731,6 +754,8 @@ void launch_motion_cfl(const Dev& D, cudaStream_t s) {
   pdl_launch(k_cfl, grid_for(D.N), NT, 0, s, D);
   if (D.coastal) pdl_launch(k_wave_tables, wt, NT, 0, s, D, 1);
   pdl_launch(k_compress, grid_for(D.N), NT, 0, s, D);
+  const long long staged = D.NF + D.N;
+  pdl_launch(k_stage_candidate, grid_for(D.N % 4 == 0 && staged % 4 == 0 ? staged / 4 : staged), NT, 0, s, D);
 }
 void launch_sweep(const Dev& D, cudaStream_t s) {
   pdl_launch(k_sweep_plane, grid_for(D.N), NT, 0, s, D);

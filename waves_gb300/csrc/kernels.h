@@ -95,6 +95,7 @@ void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds);
 void launch_mg_build(const Dev& D, cudaStream_t s);
 void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase);
 void mg_kernel_attributes();
+int coarse_blocks(size_t smem);  // blocks of the one-launch coarse V-cycle, 0 when unavailable
 void launch_mg_cols(const Dev& D, cudaStream_t s);
 // k_init.cu
 void launch_initial(const Dev& D, cudaStream_t s, float4* probes);

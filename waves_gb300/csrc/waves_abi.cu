@@ -504,9 +504,31 @@ waves_status setup_device(waves_handle* h) {
     const int lb = D.mg_bottom, Lc = D.L - 1;
     const size_t span = (size_t)D.lv[Lc].off + D.lv[Lc].count - D.lv[lb].off;
     const size_t rows = (size_t)(D.lv[Lc].eoff + (long long)D.lv[Lc].stencil * D.lv[Lc].count - D.lv[lb].eoff);
-    const size_t bytes = ((8 * span * tsz + 15) & ~(size_t)15) + rows * tsz;
-    D.mg_bottom_smem = lb >= 1 && bytes <= (size_t)wg::kBottomSmemMax ? (int)bytes : 0;
+    const size_t bytes = ((8 * span * tsz + 15) & ~(size_t)15) + ((rows * tsz + 15) & ~(size_t)15) + rows * 2;
+    bool narrow = true;  // every staged level indexable in 16 bits
+    for (int l = lb; l <= Lc; l++) narrow = narrow && D.lv[l].count <= 65536;
+    D.mg_bottom_smem = lb >= 1 && narrow && bytes <= (size_t)wg::kBottomSmemMax ? (int)bytes : 0;
     if (getenv("WAVES_MG_BOTTOM_GLOBAL")) D.mg_bottom_smem = 0;
+  }
+  {
+    // WAVES_MG_COARSE=1: the coarse levels (fewer than 65536 rows) above the bottom run as one
+    // cooperative launch.  Off by default: on the beach it removes about 230 launches per trial
+    // but is no faster than the per-level launches (14.05 vs 13.93 ms per step).
+    D.mg_coarse_from = 0;
+    if (const char* e = getenv("WAVES_MG_COARSE"))
+      if (atoi(e) != 0)
+        for (int l = 1; l < D.mg_bottom; l++)
+          if (D.lv[l].count < 65536) {
+            D.mg_coarse_from = l;
+            break;
+          }
+    if (D.mg_coarse_from > 0) {
+      wg::mg_kernel_attributes();
+      const size_t smem = std::max((size_t)wg::kMaxStencil * 64 * sizeof(float), (size_t)D.mg_bottom_smem);
+      D.coarse_blocks = wg::coarse_blocks(smem);
+      if (D.coarse_blocks <= 0) D.mg_coarse_from = 0;
+    }
+    AL(D.gbar, 2, false, "grid_barrier");
   }
   AL(D.mgmat, moff, true, "mg_matrix");
   {

@@ -1,0 +1,111 @@
+/*
+ * waves_run: headless driver of the waves solver step through the C ABI only (include/waves.h).
+ *
+ *   waves_run [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16]
+ *             [--frame DT] [--surface FILE]
+ *
+ * It plays the role of the reference's lab runner (water/lab_runner.gd:49-73): it requests
+ * accepted time frame by frame (1/60 s by default, request_time), runs the solver until each
+ * frame's quota is met, and prints one JSON line per run with the telemetry of waves_stats and
+ * the device time of waves_timing.  --surface writes the last accepted surface export (float4
+ * planes then float kinds, ops 19/14) to a file.  The exit status is 0 on success, 1 on a bad
+ * argument, 2 when the library fails, 3 when the solver halts.
+ */
+#define _POSIX_C_SOURCE 199309L
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "waves.h"
+
+static double now_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+int main(int argc, char** argv) {
+  const char* preset = "beach";
+  const char* surface = NULL;
+  double seconds = 1.0, frame = 1.0 / 60.0, tol = 1e-6;
+  long steps = 0;
+  int mg = 32;
+  for (int i = 1; i < argc; i++) {
+    const char* a = argv[i];
+    const char* v = i + 1 < argc ? argv[i + 1] : NULL;
+    if (!strcmp(a, "--preset") && v) preset = v, i++;
+    else if (!strcmp(a, "--seconds") && v) seconds = atof(v), i++;
+    else if (!strcmp(a, "--steps") && v) steps = atol(v), i++;
+    else if (!strcmp(a, "--tol") && v) tol = atof(v), i++;
+    else if (!strcmp(a, "--mg") && v) mg = atoi(v), i++;
+    else if (!strcmp(a, "--frame") && v) frame = atof(v), i++;
+    else if (!strcmp(a, "--surface") && v) surface = v, i++;
+    else {
+      fprintf(stderr, "usage: %s [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16] "
+                      "[--frame DT] [--surface FILE]\n", argv[0]);
+      return 1;
+    }
+  }
+  waves_config cfg;
+  if (!strcmp(preset, "beach")) waves_config_beach(&cfg);
+  else if (!strcmp(preset, "tank")) waves_config_tank(&cfg);
+  else if (!strcmp(preset, "default")) waves_config_default(&cfg);
+  else {
+    fprintf(stderr, "unknown preset %s\n", preset);
+    return 1;
+  }
+  cfg.pressure_tolerance = (float)tol;
+  cfg.mg_precision = mg;
+  waves_handle* h = NULL;
+  waves_status st = waves_create(&cfg, &h);
+  if (st != WAVES_OK) {
+    fprintf(stderr, "waves_create: %d %s\n", (int)st, waves_last_error(NULL));
+    return 2;
+  }
+  int halted = 0;
+  const double t0 = now_s();
+  if (steps > 0) {
+    waves_request_steps(h, steps);
+    st = waves_run(h, 4);
+    halted = st == WAVES_SOLVER_FAILED;
+  } else {
+    for (double t = frame; t <= seconds + 1e-9 && !halted; t += frame) {
+      waves_request_time(h, t);
+      st = waves_run(h, 4);
+      halted = st == WAVES_SOLVER_FAILED;
+    }
+  }
+  if (st != WAVES_OK && !halted) {
+    fprintf(stderr, "waves_run: %d %s\n", (int)st, waves_last_error(h));
+    waves_destroy(h);
+    return 2;
+  }
+  waves_synchronize(h);
+  const double wall = now_s() - t0;
+  waves_stats_t s;
+  waves_stats(h, &s);
+  double motion_ms = 0, pressure_ms = 0;
+  int64_t trials = 0;
+  waves_timing(h, &motion_ms, &pressure_ms, &trials, 0);
+  printf("{\"preset\": \"%s\", \"n\": [%d, %d, %d], \"accepted_steps\": %lld, \"accepted_time\": %.9g, "
+         "\"trials\": %lld, \"failure\": %d, \"wall_s\": %.6g, \"sim_s_per_wall_s\": %.6g, "
+         "\"device_motion_ms\": %.6g, \"device_pressure_ms\": %.6g}\n",
+         preset, cfg.n[0], cfg.n[1], cfg.n[2], (long long)s.accepted_steps, s.accepted_time, (long long)trials,
+         (int)s.failure, wall, wall > 0 ? s.accepted_time / wall : 0.0, motion_ms, pressure_ms);
+  if (surface) {
+    const size_t n = (size_t)cfg.n[0] * cfg.n[1] * cfg.n[2];
+    float* planes = (float*)malloc(n * 4 * sizeof(float));
+    float* kinds = (float*)malloc(n * sizeof(float));
+    FILE* f = planes && kinds ? fopen(surface, "wb") : NULL;
+    if (f && waves_export_surface(h, planes, kinds) == WAVES_OK) {
+      fwrite(planes, sizeof(float), n * 4, f);
+      fwrite(kinds, sizeof(float), n, f);
+    }
+    if (f) fclose(f);
+    free(planes);
+    free(kinds);
+  }
+  waves_destroy(h);
+  return halted ? 3 : 0;
+}
