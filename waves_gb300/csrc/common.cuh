@@ -50,12 +50,13 @@ DI float clampf_(float x, float lo, float hi) { return mnf(mxf(x, lo), hi); }
 DI float fract_(float x) { return x - floorf(x); }
 DI float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
 // griddepcontrol.wait: returns once the grid this one depends on (programmatic launch) has
-// completed and its memory is visible (immediate for a normally launched kernel); then
-// griddepcontrol.launch_dependents lets the next kernel on the stream be scheduled once every
-// block of this grid is resident (it still waits for this grid to complete before it reads).
-DI void grid_dep_wait() {
+// completed and its memory is visible (immediate for a normally launched kernel).  With `early`,
+// griddepcontrol.launch_dependents then lets the next kernel be scheduled as soon as every block
+// of this grid is resident; without it the next kernel launches as this grid exits.  On the beach
+// the exit trigger is the faster (13.23 vs 13.86 ms per step; 13.48 without programmatic launch).
+DI void grid_dep_wait(int early) {
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (early) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 DI float tcos(float x) { return (float)cos((double)x); }
 DI float tsin(float x) { return (float)sin((double)x); }

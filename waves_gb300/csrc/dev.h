@@ -114,6 +114,7 @@ struct Dev {
   int* mac_list;                 // MacCormack work list (faces)
   unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
   int mac_grid;                  // persistent MacCormack blocks
+  int pdl_early;                 // kernels trigger their dependents' launch on entry
   // learned warm start (allocated when warm_start is configured): weights in mma fragment order,
   // biases [4][16], scales (F, b, p_prev inputs; output), BF16 activations [2][N][16], p_net [N]
   int net_on;

@@ -224,7 +224,7 @@ DI bool post_on(const Dev& D) { return D.c[4] > .5 && D.c[6] > .5 && D.c[7] < .5
 
 // ---------------------------------------------------------------- op 17 (+ coastal op 87/88)
 __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D, int op, int with_bounds) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   bool on = op == 19 ? !(D.c[4] > .5) : geometry_on(D);
   bool bounds = with_bounds && setup_on(D);
   if (!on && !bounds) return;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- op 18
 __global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!geometry_on(D)) return;
   Geo G(D, 18);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) 
 
 // ---------------------------------------------------------------- op 16
 __global__ void __launch_bounds__(NT) k_geom_coef(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!geometry_on(D)) return;
   Geo G(D, 16);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(NT) k_geom_coef(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- op 2 + op 47
 __global__ void __launch_bounds__(NT) k_proj_setup(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!(D.c[5] > .5)) return;
   Geo G(D, 2);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(NT) k_proj_setup(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- op 11 (gradient apply)
 __global__ void __launch_bounds__(NT) k_grad_apply(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!post_on(D)) return;
   Geo G(D, 11);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(NT) k_grad_apply(const __grid_constant__ Dev D
 
 // ---------------------------------------------------------------- ops 30-33 (nearest sources)
 __global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(NT) k_ext_init(const __grid_constant__ Dev D) 
 // Static neighbourhood of every face for the extension hops: bit 6 set for a wall face, bit
 // 2a + (sign > 0) set when the neighbour along axis a is in bounds and not a wall face.
 __global__ void __launch_bounds__(NT) k_ext_masks(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
   if (f >= D.NF) return;
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(NT) k_ext_masks(const __grid_constant__ Dev D)
   D.ext_nb[f] = (unsigned char)bits;
 }
 __global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, int rb) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!post_on(D)) return;
   Grid g(D);
   long long f = (long long)blockIdx.x * NT + threadIdx.x;
@@ -429,7 +429,7 @@ DI float extended_value(const Dev& D, const Grid& g, const float* Cb, int packed
 
 // ---------------------------------------------------------------- op 34 + 47 + 48
 __global__ void __launch_bounds__(NT) k_ext_write(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!post_on(D)) return;
   Grid g(D);
   int cand = 1 - acc_bank(D);
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(NT) k_ext_write(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- ops 35/36, 62/66, 65, 12/13
 __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!post_on(D)) return;
   Geo G(D, 12);
   const Grid& g = G.g;
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- ops 44, 85, 89 (one block)
 __global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   __shared__ float cols[8 * 128];
   Grid g(D);
   const float* A = bank_ptr(D, acc_bank(D));
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- coastal ops 80-84
 __global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Geo G(D, 80);
   const Grid& g = G.g;
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(NT) k_coast_cells(const __grid_constant__ Dev 
   }
 }
 __global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Geo G(D, 82);
   const Grid& g = G.g;
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(NT) k_coast_faces(const __grid_constant__ Dev 
   D.fwd[f] = value - old;
 }
 __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Geo G(D, 83);
   const Grid& g = G.g;
@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ D
 
 // ---------------------------------------------------------------- export (op 19) into buffers
 __global__ void __launch_bounds__(NT) k_export(const __grid_constant__ Dev D, float4* planes, float* kinds) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   Geo G(D, 19);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;

@@ -10,7 +10,7 @@ constexpr int NT = 256;
 
 // op 0 (pressure_pass.glslinc:182-198)
 __global__ void __launch_bounds__(NT) k_init_still(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.S) return;
@@ -44,7 +44,7 @@ DI float block_overlap(const Dev& D, F3 lo, F3 hi, F3 lower, F3 upper) {
 }
 // op 40 (coupled_motion.glslinc:234-270)
 __global__ void __launch_bounds__(NT) k_init_fixture(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   int shape = D.shape;
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(NT) k_init_fixture(const __grid_constant__ Dev
 
 // op 41/42
 __global__ void __launch_bounds__(NT) k_init_volume(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   double v[1] = {0};
   if (i < D.N) v[0] = (double)bank_ptr(D, acc_bank(D))[i] * D.cell_d;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(NT) k_init_volume(const __grid_constant__ Dev 
 
 // op 49 (coupled_motion.glslinc:323-337)
 __global__ void __launch_bounds__(NT) k_init_masks(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i < D.N) {
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(NT) k_init_masks(const __grid_constant__ Dev D
 
 // op 86 (coastal_pass.glslinc:78-83)
 __global__ void k_probes(const __grid_constant__ Dev D, float4* out) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   int i = threadIdx.x;
   if (i >= 8) return;
   Coast cs(D);

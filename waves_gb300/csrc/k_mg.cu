@@ -191,7 +191,7 @@ DI unsigned signature(const Dev& D, const Grid& g, long long i) {
   return result;
 }
 __global__ void k_hs_reset(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   for (int k = 1; k <= 7; k++) s[k] = 0;
@@ -203,7 +203,7 @@ __global__ void k_hs_reset(const __grid_constant__ Dev D) {
 struct AddU { DI unsigned operator()(unsigned a, unsigned b) const { return a + b; } };
 struct MaxU { DI unsigned operator()(unsigned a, unsigned b) const { return a < b ? b : a; } };
 __global__ void __launch_bounds__(NT) k_hs_count(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   __shared__ unsigned sh[32];
   Grid g(D);
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(NT) k_hs_count(const __grid_constant__ Dev D) 
   }
 }
 __global__ void k_hs_decide(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   double* c = D.c;
@@ -272,7 +272,7 @@ __global__ void k_hs_decide(const __grid_constant__ Dev D) {
   }
 }
 template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -296,7 +296,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_hs_snapshot(const __g
   }
 }
 __global__ void k_hs_record(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   unsigned* s = D.hstate;
   if (s[13] <= (unsigned)D.hist_cap) {
@@ -307,7 +307,7 @@ __global__ void k_hs_record(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- build ops
 template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[9] == 0) return;
   __shared__ unsigned sh[32];
   MG m(D);
@@ -339,12 +339,12 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_mask(const __grid_
 // prolongation adds at active cells only, so the rows skipped never reach level 0 (their
 // iterates stay at the zero the restriction writes).  Warps append contiguously.
 __global__ void k_mg_rows_reset(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   if (threadIdx.x < kMaxLevels) D.mg_rowcount[threadIdx.x] = 0u;
 }
 template <class T> __global__ void __launch_bounds__(NT) k_mg_rowlist(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D)) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -358,7 +358,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_rowlist(const __gr
   if (act) D.mg_rowlist[lv.off + base + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || !(D.hstate[14] == 0 || D.hstate[20 + l + 1] != 0)) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -374,7 +374,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __g
 }
 // l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -413,7 +413,7 @@ DI void child_range(const Dev& D, int l, int axis, int qc, int& lo, int& ext) {
 }
 // Deterministic Galerkin product of level l into level l+1 (replaces ops 2 + 3).
 template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __grid_constant__ Dev D, int l, int ex, int ey, int ez) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   extern __shared__ float part[];  // [125][GT]
   MG m(D);
@@ -474,7 +474,7 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
 }
 // ELL rows (pressure_multigrid.glslinc:176-182)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
@@ -491,7 +491,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_c
 }
 // Dense Cholesky and L^-1 of the last level (pressure_mg_coarse.glslinc:34-48), one block.
 template <class T> __global__ void k_mg_chol(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   __shared__ float dense[64 * 64];
   __shared__ float inv[64 * 64];
@@ -731,7 +731,7 @@ template <class T> DI float apply0(const Dev& D, const T* __restrict__ x, const 
 template <class T>
 __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, int phase, int source, float c1, float c2,
                                                   int first_k, int src_zero, int fin) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   const Cell0 c = cell0(D);
   double v[4] = {0, 0, 0, 0};
@@ -767,7 +767,7 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
   }
 }
 template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __grid_constant__ Dev D, int phase, int f) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   const Cell0 c = cell0(D);
   if (!c.ok) return;
@@ -775,7 +775,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __
 }
 // phase 0 load (op 5 of the cycle) fused with the first Chebyshev sweep from zero
 template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid_constant__ Dev D, int phase, int first_sweep) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -795,7 +795,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
 
 // Generic levels (l >= 1): one thread per cell.
 template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   __shared__ int lin[kMaxStencil];
   const int* lin_s = nullptr;
@@ -823,7 +823,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_cons
 // Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a level >= 1 with the
 // product-parallel apply: RR rows per block.
 template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   __shared__ float prod[kMaxStencil * RR];
   __shared__ bool inner[RR];
@@ -918,7 +918,7 @@ template <class T, class M> DI void bottom_cycle(const Dev& D, const M& m, int l
   }
 }
 template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __grid_constant__ Dev D, int phase, int lb) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   __shared__ float small[64];
   bottom_cycle<T>(D, MG(D), lb, small);
@@ -950,7 +950,7 @@ template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* st
     for (int k = threadIdx.x; k < span; k += blockDim.x) out[(size_t)f * D.mg_nodes + k] = vec[f * span + k];
 }
 template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom_smem(const __grid_constant__ Dev D, int phase, int lb) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   extern __shared__ __align__(16) unsigned char stage[];
   __shared__ float small[64];
@@ -996,7 +996,7 @@ DI void grid_barrier(const Dev& D) {
 
 template <class T>
 __global__ void __launch_bounds__(CNT) k_mg_coarse(const __grid_constant__ Dev D, int phase, int lt) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;  // the same decision in every block
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ bool inner[CRR];
@@ -1059,7 +1059,7 @@ __global__ void __launch_bounds__(CNT) k_mg_coarse(const __grid_constant__ Dev D
 
 // op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __grid_constant__ Dev D, int phase, int f) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -1213,7 +1213,7 @@ template <class T> struct Cycle {
 
 // Columns of the ELL rows, max(wrap(l, q + offset), 0), computed once (static geometry).
 __global__ void __launch_bounds__(NT) k_mg_cols(const __grid_constant__ Dev D, int l) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
   int i = blockIdx.x * NT + threadIdx.x;
@@ -1228,7 +1228,7 @@ __global__ void __launch_bounds__(NT) k_mg_cols(const __grid_constant__ Dev D, i
 // Level-0 neighbour-active bits (bit f: neighbour across face f active, bit 6: cell active),
 // rebuilt after the masks on structural rebuilds.
 template <class T> __global__ void __launch_bounds__(NT) k_mg_nb0(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[9] == 0) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;

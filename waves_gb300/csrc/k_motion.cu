@@ -78,7 +78,7 @@ DI bool setup_on(const Dev& D) { return D.c[5] > .5 && D.c[7] < .5; }
 // which 0: the accepted time and the CFL look-ahead time (before op 20); which 1: the new time
 // c1 + dt and the relaxation factors at dt (after op 20 has set dt).  One thread per (column, row).
 __global__ void __launch_bounds__(NT) k_wave_tables(const __grid_constant__ Dev D, int which) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   const Grid g(D);
   const Coast cs(D);
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(NT) k_wave_tables(const __grid_constant__ Dev 
 
 // ---------------------------------------------------------------- op 20/21
 __global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- op 45/46 + c_i of op 22
 __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
   const float* pmA = m.acc == 0 ? D.pmask0 : D.pmask1;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) 
 // but a trial that fails before them (CFL, compression, sweep bounds) leaves this copy, as the
 // reference does.  c_i is set by k_compress.
 __global__ void __launch_bounds__(NT) k_stage_candidate(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   const int acc = acc_bank(D);
   const float4* src = reinterpret_cast<const float4*>(bank_ptr(D, acc) + D.N);
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(NT) k_stage_candidate(const __grid_constant__ 
 
 // ---------------------------------------------------------------- op 23
 __global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -226,7 +226,7 @@ DI float sweep_flux(const Motion& m, I3 q, int axis, float& courant) {
 
 // ---------------------------------------------------------------- op 24 + 55/56 + 25/26
 __global__ void __launch_bounds__(NT) k_sweep_update(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
   int sa = ((int)D.c[2] + (int)D.c[21]) % 3;
@@ -639,11 +639,11 @@ template <int op, bool cached> DI void mac_face(const Dev& D, const Motion& m, c
 // warp appends its faces contiguously.  A face that does not advect gets its op 27/28 results
 // (zero) here.  mac_ctr: [0] interior count, [1] boundary count, [2]/[3] op 27/28 work cursors.
 __global__ void k_mac_reset(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (threadIdx.x < 4) D.mac_ctr[threadIdx.x] = 0u;
 }
 __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
   const float* vb = m.acc == 0 ? D.vband0 : D.vband1;
@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) 
 // Persistent pass over the work list: each warp takes 32 consecutive entries at a time, boundary
 // faces first, so a slow warp never holds idle lanes of a finished block.
 template <int op, bool cached> __global__ void __launch_bounds__(NT) k_mac(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   const unsigned n_int = D.mac_ctr[0], n_edge = D.mac_ctr[1], total = n_int + n_edge;
   unsigned* cursor = D.mac_ctr + (op == 27 ? 2 : 3);

@@ -47,7 +47,7 @@ DI uint32_t pack_bf16(float lo, float hi) {
 // Weights arrive in mma fragment order: [tap][n-tile][lane][2] packed BF16 pairs.
 template <int LAYER>
 __global__ void __launch_bounds__(NT) k_net_layer(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!warm_on(D)) return;
   constexpr int NTILES = LAYER == 3 ? 1 : 2;
   __shared__ __align__(16) __nv_bfloat16 tile[kHalo * kStride];

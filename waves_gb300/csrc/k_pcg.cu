@@ -34,7 +34,7 @@ DI float operator_at(const Dev& D, const Grid& g, I3 q, long long i, const float
 DI bool warm_on(const Dev& D) { return D.c[kNetLoaded] > .5 && D.c[5] > .5 && D.c[7] < .5; }
 // b of op 3 (pressure_iterations.glslinc) ahead of the network, the same expression as k_cg_init
 __global__ void __launch_bounds__(NT) k_warm_rhs(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!warm_on(D)) return;
   Grid g(D);
   const float* Cb = bank_ptr(D, 1 - acc_bank(D));
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(NT) k_warm_rhs(const __grid_constant__ Dev D) 
 // |b - A p_prev|^2 and |b - A p_net|^2 over wet cells (FP64); the network's pressure is taken
 // only when its residual is smaller, so plain MGPCG stays the fallback.
 __global__ void __launch_bounds__(NT) k_warm_decide(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!warm_on(D)) return;
   Grid g(D);
   const float* p = bank_ptr(D, 1 - acc_bank(D)) + D.N + D.NF;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(NT) k_warm_decide(const __grid_constant__ Dev 
   }
 }
 __global__ void __launch_bounds__(NT) k_warm_apply(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!warm_on(D) || !(D.c[kWarmPick] > .5)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -90,7 +90,7 @@ namespace {
 
 // ---------------------------------------------------------------- op 3 (+ op 4 when the V-cycle is off)
 __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!pressure_setup(D)) return;
   Grid g(D);
   const float* Cb = bank_ptr(D, 1 - acc_bank(D));
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
 
 // ---------------------------------------------------------------- op 5 + 6 + 7
 __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!solving(D)) return;
   Grid g(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D)
 
 // ---------------------------------------------------------------- op 8 + multigrid load (op 5 of the cycle)
 template <class T> __global__ void __launch_bounds__(NT) k_cg_update(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   if (!solving(D)) return;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   if (i >= D.N) return;
@@ -178,7 +178,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_cg_update(const __gri
 
 // ---------------------------------------------------------------- op 10 (+ loop condition)
 __global__ void __launch_bounds__(NT) k_cg_direction(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int use_handle) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   bool on = solving(D);
   if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) {
     // The body has run ops 5-10 of one iteration; continue while solving.
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(NT) k_cg_direction(const __grid_constant__ Dev
 
 // ---------------------------------------------------------------- graph conditions
 __global__ void k_set_cond(const __grid_constant__ Dev D, cudaGraphConditionalHandle h, int which) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   const double* c = D.c;
   bool v;
   if (which == kCondDefectFirst) v = true;
@@ -205,7 +205,7 @@ __global__ void k_set_cond(const __grid_constant__ Dev D, cudaGraphConditionalHa
 
 // ---------------------------------------------------------------- ops 43 + 1 (trial begin) and 63/64
 __global__ void k_begin(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   double* c = D.c;
   // op 43 (coupled_motion.glslinc:351-355)
   bool retry = c[7] == 20 || (c[7] >= 10 && c[7] <= 12);
@@ -222,7 +222,7 @@ __global__ void k_begin(const __grid_constant__ Dev D) {
   }
 }
 __global__ void __launch_bounds__(NT) k_defect_begin(const __grid_constant__ Dev D) {
-  grid_dep_wait();
+  grid_dep_wait(D.pdl_early);
   const double* c = D.c;
   double c57 = c[57];
   bool go = (c57 == 1 || c57 == 2) && c[7] < .5;

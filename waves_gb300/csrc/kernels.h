@@ -47,7 +47,8 @@ template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launc
 // Programmatic dependent launch: a kernel launched this way may be scheduled while the previous
 // kernel on the stream drains; every kernel's first statement is grid_dep_wait()
 // (griddepcontrol.wait), which returns once that kernel has completed and its writes are visible,
-// so only launch latency overlaps.  On by default; WAVES_PDL=0 at handle creation turns it off.
+// so only launch latency overlaps.  WAVES_PDL at handle creation: 0 off, 1 on (default), 2 on with
+// the early trigger (kernels release their dependents on entry).
 // With a probe list installed, every launch is also bracketed as kind kProbeAll.
 extern bool g_pdl;
 template <class... KArgs, class... Args>

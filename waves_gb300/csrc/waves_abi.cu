@@ -364,6 +364,8 @@ waves_status setup_device(waves_handle* h) {
   AL(D.mac_list, NF, false, "mac_list");
   AL(D.mac_ctr, 4, false, "mac_counters");
   D.mac_grid = wg::mac_blocks();
+  D.pdl_early = 0;
+  if (const char* e = getenv("WAVES_PDL")) D.pdl_early = atoi(e) == 2;
   if (D.mac_grid <= 0) D.mac_grid = 2 * 152;
   // multigrid
   plan_levels(h);
@@ -807,7 +809,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
   }
   waves_handle* h = new waves_handle;
   h->cfg = *cfg;
-  if (const char* e = getenv("WAVES_PDL")) wg::g_pdl = atoi(e) != 0;
+  if (const char* e = getenv("WAVES_PDL")) wg::g_pdl = atoi(e) != 0;  // 0 off, 1 on, 2 on with the early trigger
   waves_status st = WAVES_OK;
   auto fail = [&](waves_status s) {
     g_create_error = h->err;
