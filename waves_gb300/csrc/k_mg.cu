@@ -794,17 +794,18 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
 }
 
 // Generic levels (l >= 1): one thread per cell.
-template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+template <class T, int NTB = NT>
+__global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   __shared__ int lin[kMaxStencil];
   const int* lin_s = nullptr;
   if (op <= 2 && l >= 1) {
-    for (int k = threadIdx.x; k < D.lv[l].stencil; k += NT) lin[k] = __ldg(D.stencil_lin + D.lv[l].soff + k);
+    for (int k = threadIdx.x; k < D.lv[l].stencil; k += NTB) lin[k] = __ldg(D.stencil_lin + D.lv[l].soff + k);
     __syncthreads();
     lin_s = lin;
   }
-  int i = blockIdx.x * NT + threadIdx.x;
+  int i = blockIdx.x * NTB + threadIdx.x;
   if (l >= 1 && op != 3) {  // sweeps, residual, prolongation: active rows only
     if (i >= (int)D.mg_rowcount[l]) return;
     i = D.mg_rowlist[D.lv[l].off + i];
@@ -822,24 +823,25 @@ template <class T> __global__ void __launch_bounds__(NT) k_mgl(const __grid_cons
 
 // Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a level >= 1 with the
 // product-parallel apply: RR rows per block.
-template <class T> __global__ void __launch_bounds__(NT) k_mgl_rows(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+template <class T, int RRB = RR>
+__global__ void __launch_bounds__(NT) k_mgl_rows(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
-  __shared__ float prod[kMaxStencil * RR];
-  __shared__ bool inner[RR];
+  __shared__ float prod[kMaxStencil * RRB];
+  __shared__ bool inner[RRB];
   __shared__ int lin[kMaxStencil];
-  __shared__ int rowi[RR];
-  const int row0 = blockIdx.x * RR, nrows = (int)D.mg_rowcount[l];
+  __shared__ int rowi[RRB];
+  const int row0 = blockIdx.x * RRB, nrows = (int)D.mg_rowcount[l];
   if (row0 >= nrows) return;  // uniform over the block
   MG m(D);
-  if (threadIdx.x < RR) rowi[threadIdx.x] = row0 + threadIdx.x < nrows ? D.mg_rowlist[D.lv[l].off + row0 + threadIdx.x] : -1;
+  if (threadIdx.x < RRB) rowi[threadIdx.x] = row0 + threadIdx.x < nrows ? D.mg_rowlist[D.lv[l].off + row0 + threadIdx.x] : -1;
   __syncthreads();
   const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);
-  if (need) row_products<T>(m, l, a, rowi, prod, inner, lin);
-  if (threadIdx.x >= RR) return;
+  if (need) row_products<T, NT, RRB>(m, l, a, rowi, prod, inner, lin);
+  if (threadIdx.x >= RRB) return;
   const int i = rowi[threadIdx.x];
   if (i < 0) return;
-  const float ax = need ? row_sum<T>(m, l, a, i, prod) : 0.f;
+  const float ax = need ? row_sum<T, RRB>(m, l, a, i, prod) : 0.f;
   switch (op) {
     case 0: cheb_update<T>(m, l, a, b, i, c != 0, ax); break;
     case 1: jacobi_update<T>(m, l, a, b, i, ax); break;
@@ -1136,16 +1138,26 @@ template <class T> struct Cycle {
   cudaStream_t s;
   int phase;
   int fused_first;  // the level-0 first pre-smoothing sweep was done by the caller
-  unsigned rows_grid(int l) const { return (unsigned)((D.lv[l].count + RR - 1) / RR); }
+  unsigned rows_grid(int l, int rr) const { return (unsigned)((D.lv[l].count + rr - 1) / rr); }
   // Levels with few rows use the product-parallel kernel (enough independent loads in flight);
   // larger levels keep one thread per row.
   bool few_rows(int l) const { return D.lv[l].count < D.mg_rows_below; }
   void level_op(int l, int op, int a, int b, int c) {
     const double bytes = level_op_bytes(D, l, op, b, c, sizeof(T));
     if (few_rows(l))
-      probed(kProbeRows, s, bytes, [&] { pdl_launch((k_mgl_rows<T>), rows_grid(l), NT, 0, s, D, phase, op, l, a, b, c); });
+      probed(kProbeRows, s, bytes, [&] {
+        if (D.mg_rows_rr == 8) pdl_launch((k_mgl_rows<T, 8>), rows_grid(l, 8), NT, 0, s, D, phase, op, l, a, b, c);
+        else if (D.mg_rows_rr == 16) pdl_launch((k_mgl_rows<T, 16>), rows_grid(l, 16), NT, 0, s, D, phase, op, l, a, b, c);
+        else if (D.mg_rows_rr == 64) pdl_launch((k_mgl_rows<T, 64>), rows_grid(l, 64), NT, 0, s, D, phase, op, l, a, b, c);
+        else pdl_launch((k_mgl_rows<T, RR>), rows_grid(l, RR), NT, 0, s, D, phase, op, l, a, b, c);
+      });
     else
-      probed(kProbeRowThread, s, bytes, [&] { pdl_launch((k_mgl<T>), grid_for(D.lv[l].count), NT, 0, s, D, phase, op, l, a, b, c); });
+      probed(kProbeRowThread, s, bytes, [&] {
+        if (D.mg_thread_nt == 128)
+          pdl_launch((k_mgl<T, 128>), (unsigned)((D.lv[l].count + 127) / 128), 128, 0, s, D, phase, op, l, a, b, c);
+        else
+          pdl_launch((k_mgl<T, NT>), grid_for(D.lv[l].count), NT, 0, s, D, phase, op, l, a, b, c);
+      });
   }
   dim3 grid0() const { return dim3((unsigned)((D.nx + kTileX - 1) / kTileX), (unsigned)((D.ny + kTileY - 1) / kTileY), (unsigned)D.nz); }
   int smooth(int l, int field, bool zero, bool last0) {

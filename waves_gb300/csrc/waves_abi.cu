@@ -501,6 +501,16 @@ waves_status setup_device(waves_handle* h) {
   // Levels with fewer rows than this use the product-parallel apply (both forms give the same bits).
   D.mg_rows_below = 65536;
   if (const char* e = getenv("WAVES_MG_ROWS_BELOW")) D.mg_rows_below = std::max(0, atoi(e));
+  // launch shapes of the level >= 1 sweeps (measured on the beach, ms per step over 120 steps:
+  // 16 rows per product-parallel block 13.45-13.48, 8 rows 13.67-13.70, 32 rows 13.72, 64 rows
+  // 14.52; 128-thread one-row-per-thread blocks 0.2 % faster than 256)
+  D.mg_thread_nt = 128;
+  if (const char* e = getenv("WAVES_MG_THREAD_NT")) D.mg_thread_nt = atoi(e) == 256 ? 256 : 128;
+  D.mg_rows_rr = 16;
+  if (const char* e = getenv("WAVES_MG_ROWS_RR")) {
+    const int v = atoi(e);
+    D.mg_rows_rr = (v == 8 || v == 32 || v == 64) ? v : 16;
+  }
   {
     // levels mg_bottom..L-1 staged in shared memory when their fields and rows fit
     const int lb = D.mg_bottom, Lc = D.L - 1;
