@@ -363,7 +363,9 @@ struct Mac {
   // lo is inside the domain and no solid cell lies in the 3x3 (x, y) window around it, every
   // donor is a plain stored face (no reflection, ghost or wall branch applies, parity 1), so the
   // donor lookups reduce to two loads each; the arithmetic is unchanged.
-  DI float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
+  // With want_value false only `valid` is produced (the value and limits are not needed): the
+  // fast path then skips the eight value loads.
+  DI float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1, bool want_value = true) const {
     const Dev& D = m.D;
     F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);
     lattice[axis] += .5f;
@@ -385,7 +387,7 @@ struct Mac {
         int qz = pidx(lo.z + z, D.nz);  // wrap; a face at z = nz is the canonical z = 0
         long long f = base + (long long)(lo.x + xx) + (long long)mx_ * ((long long)(lo.y + y) + (long long)my_ * qz);
         bool supported = vb[f] > .5f;
-        float value = src[f];
+        float value = want_value ? src[f] : 0.f;
         values[c] = value;
         float wx = xx ? t.x : 1.f - t.x, wy = y ? t.y : 1.f - t.y, wz = z ? t.z : 1.f - t.z;
         if (wx * wy * wz > 0.f) {
@@ -530,7 +532,7 @@ DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float*
     for (int a = 0; a < 3; a++) {
       bool valid;
       float lo, hi;
-      const float s = mc.sample(p, a, false, valid, lo, hi);
+      const float s = mc.sample(p, a, false, valid, lo, hi, stage < 2 || a == axis);
       if (!valid) ok &= ~(1u << stage);
       if (a == 0) v0 = s;
       else if (a == 1) v1 = s;
@@ -586,7 +588,7 @@ DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
     for (int a = 0; a < 3; a++) {
       bool valid;
       float lo, hi;
-      const float s = mc.sample(p, a, stage == 1 && a == axis, valid, lo, hi);
+      const float s = mc.sample(p, a, stage == 1 && a == axis, valid, lo, hi, stage == 0 || a == axis);
       ok = ok && valid;
       if (a == 0) v0 = s;
       else if (a == 1) v1 = s;
