@@ -113,7 +113,9 @@ struct Dev {
   unsigned char* ext_nb;         // per face: wall bit and usable extension neighbours (static)
   int* mac_list;                 // MacCormack work list (faces)
   unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
-  int mac_grid;                  // persistent MacCormack blocks
+  int mac_grid;                  // persistent MacCormack blocks (3 per SM form)
+  int mac_grid2;                 // the same, 2 per SM form
+  int mac_minb;                  // which form runs (2 or 3 blocks per SM)
   int pdl_early;                 // kernels trigger their dependents' launch on entry
   // learned warm start (allocated when warm_start is configured): weights in mma fragment order,
   // biases [4][16], scales (F, b, p_prev inputs; output), BF16 activations [2][N][16], p_net [N]

@@ -679,7 +679,8 @@ __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) 
 }
 // Persistent pass over the work list: each warp takes 32 consecutive entries at a time, boundary
 // faces first, so a slow warp never holds idle lanes of a finished block.
-template <int op, bool cached> __global__ void __launch_bounds__(NT) k_mac(const __grid_constant__ Dev D) {
+template <int op, bool cached, int MINB = 2>
+__global__ void __launch_bounds__(NT, MINB) k_mac(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   const unsigned n_int = D.mac_ctr[0], n_edge = D.mac_ctr[1], total = n_int + n_edge;
@@ -764,10 +765,17 @@ void launch_sweep(const Dev& D, cudaStream_t s) {
   // reads F, the plane field (16 B), the sweep-axis faces and c_i; writes F
   probed(kProbeSweepVof, s, 32.0 * (double)D.N, [&] { pdl_launch(k_sweep_update, grid_for(D.N), NT, 0, s, D); });
 }
-int mac_blocks() {
+int mac_blocks2() {
   int dev = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mac<28, true>, NT, 0) != cudaSuccess)
+    return 0;
+  return sms * (per_sm > 0 ? per_sm : 1);
+}
+int mac_blocks() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mac<28, true, 3>, NT, 0) != cudaSuccess)
     return 0;
   return sms * (per_sm > 0 ? per_sm : 1);
 }
@@ -778,8 +786,13 @@ void launch_maccormack(const Dev& D, cudaStream_t s) {
   // cache, its six fields); op 28 reads those, the faces and the band, and writes the candidate.
   const double nf = (double)D.NF, cache = (D.flags & 4) ? 6.0 : 0.0;
   if (D.flags & 4) {
-    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true>), D.mac_grid, NT, 0, s, D); });
-    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true>), D.mac_grid, NT, 0, s, D); });
+    if (D.mac_minb == 3) {
+      probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true, 3>), D.mac_grid, NT, 0, s, D); });
+      probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true, 3>), D.mac_grid, NT, 0, s, D); });
+    } else {
+      probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true>), D.mac_grid2, NT, 0, s, D); });
+      probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true>), D.mac_grid2, NT, 0, s, D); });
+    }
   } else {
     probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, false>), D.mac_grid, NT, 0, s, D); });
     probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, false>), D.mac_grid, NT, 0, s, D); });

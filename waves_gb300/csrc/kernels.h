@@ -82,7 +82,8 @@ void launch_delay(cudaStream_t s, long long cycles);
 void launch_motion_cfl(const Dev& D, cudaStream_t s);
 void launch_sweep(const Dev& D, cudaStream_t s);
 void launch_maccormack(const Dev& D, cudaStream_t s);
-int mac_blocks();  // resident blocks of the persistent MacCormack kernel on the current device
+int mac_blocks();   // resident blocks of the persistent MacCormack kernel (3 per SM form)
+int mac_blocks2();  // the same for the 2-per-SM form
 void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis, int forward, float* out);
 // k_geom.cu
 void launch_coastal(const Dev& D, cudaStream_t s);

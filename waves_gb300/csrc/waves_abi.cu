@@ -367,6 +367,12 @@ waves_status setup_device(waves_handle* h) {
   D.pdl_early = 0;
   if (const char* e = getenv("WAVES_PDL")) D.pdl_early = atoi(e) == 2;
   if (D.mac_grid <= 0) D.mac_grid = 2 * 152;
+  D.mac_grid2 = wg::mac_blocks2();
+  if (D.mac_grid2 <= 0) D.mac_grid2 = 2 * 152;
+  // MacCormack: 3 blocks per SM (80 registers, a few spills) beats 2 (128 registers): 935 vs
+  // 1032 us per pass on the beach; 4 measured the same as 3
+  D.mac_minb = 3;
+  if (const char* e = getenv("WAVES_MAC_BLOCKS")) D.mac_minb = atoi(e) == 2 ? 2 : 3;
   // multigrid
   plan_levels(h);
   if ((int)h->levels.size() > wg::kMaxLevels) {
