@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
 }
 
 // ---------------------------------------------------------------- op 18
-__global__ void __launch_bounds__(NT) k_geom_phi(const __grid_constant__ Dev D) {
+__global__ void __launch_bounds__(NT, 6) k_geom_phi(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!geometry_on(D)) return;
   Geo G(D, 18);

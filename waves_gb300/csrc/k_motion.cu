@@ -182,7 +182,9 @@ __global__ void __launch_bounds__(NT) k_stage_candidate(const __grid_constant__ 
 }
 
 // ---------------------------------------------------------------- op 23
-__global__ void __launch_bounds__(NT) k_sweep_plane(const __grid_constant__ Dev D) {
+// 6 resident blocks per SM (40 registers): measured on the beach equal to or faster than the
+// register-rich forms for this and the update kernel (k_sweep_update 187 vs 195-213 us)
+__global__ void __launch_bounds__(NT, 6) k_sweep_plane(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
@@ -225,7 +227,7 @@ DI float sweep_flux(const Motion& m, I3 q, int axis, float& courant) {
 }
 
 // ---------------------------------------------------------------- op 24 + 55/56 + 25/26
-__global__ void __launch_bounds__(NT) k_sweep_update(const __grid_constant__ Dev D) {
+__global__ void __launch_bounds__(NT, 6) k_sweep_update(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
   Motion m(D);
