@@ -213,6 +213,34 @@ waves_status waves_set_masks(waves_handle* h, const float* pmask, const float* v
 waves_status waves_save(waves_handle* h, void* buffer, size_t* bytes);
 waves_status waves_load(waves_handle* h, const void* buffer, size_t bytes);
 
+/* Frame-budgeted submission (water/work_scheduler.gd:41-87): one call per rendered frame.  It
+ * folds the GPU times of finished trials into a running per-trial cost (exponential average,
+ * weight 0.25, as the reference averages its chunk costs), retires finished submissions (their
+ * control block, copied asynchronously, becomes the reported telemetry), and -- unless the solver
+ * halted, the quota is met with nothing in flight, or max_inflight submissions are unfinished --
+ * enqueues as many trials as gpu_budget_ms admits at that cost (at least one, at most max_trials,
+ * stopping early once enqueueing took cpu_budget_ms) followed by the control-block copy.  It never waits for the GPU and never changes a result. */
+typedef struct waves_frame_budget {
+  double gpu_budget_ms;  /* predicted GPU time per frame (reference default 14) */
+  int32_t max_inflight;  /* unfinished submissions allowed (reference 3, at most 8) */
+  int32_t max_trials;    /* trials per submission (reference: 96 chunks) */
+  double cpu_budget_ms;  /* host enqueue time per frame, <= 0 for none (reference 4) */
+} waves_frame_budget;
+typedef struct waves_frame_report {
+  int32_t trials_submitted;  /* this call */
+  int32_t queue_depth;       /* unfinished submissions after this call */
+  int32_t idle;              /* 1: quota met and nothing in flight */
+  int32_t halted;            /* 1: the solver stopped with a failure (stats.failure) */
+  double predicted_gpu_ms;   /* trials_submitted x trial_cost_ms */
+  double trial_cost_ms;      /* running GPU cost of one trial (0 before the first measurement) */
+  double gpu_ms_total;       /* GPU time of every trial measured so far */
+  double r_fluid;            /* GPU seconds per accepted simulated second (R_fluid) */
+  double accepted_time;      /* of the latest retired submission */
+  int64_t accepted_steps;
+  int64_t submissions_retired;
+} waves_frame_report;
+waves_status waves_frame(waves_handle* h, const waves_frame_budget* budget, waves_frame_report* report);
+
 /* Learned warm start (no reference counterpart): 4 layers of 3x3x3 convolutions,
  * channels 3 -> 16 -> 16 -> 16 -> 1, BF16 weights (raw uint16 bit patterns), FP32 biases.
  * Layout per layer: weights[co][kz][ky][kx][ci].  NULL disables it. */

@@ -109,6 +109,15 @@ class WavesSolver:
             self._ck(st)
         return st
 
+    def frame(self, gpu_budget_ms=14.0, max_inflight=3, max_trials=96, cpu_budget_ms=4.0):
+        """One frame of budgeted submission (waves_frame, after water/work_scheduler.gd:frame):
+        never waits for the GPU; returns the frame report as a dict."""
+        from .abi import WavesFrameBudget, WavesFrameReport
+        b = WavesFrameBudget(float(gpu_budget_ms), int(max_inflight), int(max_trials), float(cpu_budget_ms))
+        r = WavesFrameReport()
+        self._ck(self.lib.waves_frame(self.h, C.byref(b), C.byref(r)))
+        return r.as_dict()
+
     def synchronize(self):
         self._ck(self.lib.waves_synchronize(self.h))
 

@@ -131,6 +131,34 @@ class WavesWarmStartModel(C.Structure):
     ]
 
 
+class WavesFrameBudget(C.Structure):
+    _fields_ = [
+        ("gpu_budget_ms", C.c_double),
+        ("max_inflight", C.c_int32),
+        ("max_trials", C.c_int32),
+        ("cpu_budget_ms", C.c_double),
+    ]
+
+
+class WavesFrameReport(C.Structure):
+    _fields_ = [
+        ("trials_submitted", C.c_int32),
+        ("queue_depth", C.c_int32),
+        ("idle", C.c_int32),
+        ("halted", C.c_int32),
+        ("predicted_gpu_ms", C.c_double),
+        ("trial_cost_ms", C.c_double),
+        ("gpu_ms_total", C.c_double),
+        ("r_fluid", C.c_double),
+        ("accepted_time", C.c_double),
+        ("accepted_steps", C.c_int64),
+        ("submissions_retired", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class WavesKernelProbe(C.Structure):
     _fields_ = [
         ("kind", C.c_int32),
@@ -155,6 +183,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_request_steps",
     "waves_request_time",
     "waves_advance",
+    "waves_frame",
     "waves_run",
     "waves_synchronize",
     "waves_stream",
@@ -194,6 +223,7 @@ def declare(lib):
         "waves_request_time": (C.c_int, [h, C.c_double]),
         "waves_advance": (C.c_int, [h, C.c_int32]),
         "waves_run": (C.c_int, [h, C.c_int32]),
+        "waves_frame": (C.c_int, [h, P(WavesFrameBudget), P(WavesFrameReport)]),
         "waves_synchronize": (C.c_int, [h]),
         "waves_stream": (C.c_void_p, [h]),
         "waves_timing": (C.c_int, [h, P(C.c_double), P(C.c_double), P(C.c_int64), C.c_int32]),

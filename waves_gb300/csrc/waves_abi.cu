@@ -14,6 +14,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -76,6 +77,21 @@ struct waves_handle {
   int64_t timed_trials = 0;
   // kernels per phase: begin, setup-motion, setup-pressure, cg round set-up, cg iteration, post, end
   int32_t launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // frame-budgeted submission (waves_frame): running trial cost, unfinished submissions, each with
+  // its pinned control-block copy
+  struct Submission {
+    cudaEvent_t done;
+    int slot;
+    int trials;
+  };
+  static constexpr int kFrameSlots = 8;
+  double trial_cost_ms = 0;
+  double gpu_ms_total = 0;
+  std::vector<Submission> inflight;
+  double* frame_c = nullptr;  // pinned, kFrameSlots x WAVES_CONTROL_SIZE
+  double last_c[WAVES_CONTROL_SIZE] = {};
+  bool have_last = false;
+  int64_t serial = 0, retired = 0;
 };
 
 namespace {
@@ -733,18 +749,40 @@ cudaEvent_t take_event(waves_handle* h) {
   cudaEventCreate(&e);
   return e;
 }
+// One finished trial: totals and the running per-trial cost (work_scheduler.gd:31: weight .25,
+// floor 2 us).
+void fold_trial(waves_handle* h, float motion, float pressure) {
+  h->motion_ms += motion;
+  h->pressure_ms += pressure;
+  h->timed_trials++;
+  const double ms = (double)motion + (double)pressure;
+  h->gpu_ms_total += ms;
+  h->trial_cost_ms = h->trial_cost_ms <= 0 ? ms : h->trial_cost_ms + .25 * (std::max(ms, 0.002) - h->trial_cost_ms);
+}
 // Fold completed trial timings into the totals (called after a stream synchronisation).
 void collect_timing(waves_handle* h) {
   for (auto& t : h->ev_pending) {
     float a = 0, b = 0;
-    if (cudaEventElapsedTime(&a, t[0], t[1]) == cudaSuccess && cudaEventElapsedTime(&b, t[1], t[2]) == cudaSuccess) {
-      h->motion_ms += a;
-      h->pressure_ms += b;
-      h->timed_trials++;
-    }
+    if (cudaEventElapsedTime(&a, t[0], t[1]) == cudaSuccess && cudaEventElapsedTime(&b, t[1], t[2]) == cudaSuccess)
+      fold_trial(h, a, b);
     for (cudaEvent_t e : t) h->ev_pool.push_back(e);
   }
   h->ev_pending.clear();
+  cudaGetLastError();
+}
+// The same for the trials already finished, without waiting (stream order: stop at the first
+// unfinished one).
+void collect_timing_ready(waves_handle* h) {
+  size_t k = 0;
+  for (; k < h->ev_pending.size(); k++) {
+    auto& t = h->ev_pending[k];
+    if (cudaEventQuery(t[2]) != cudaSuccess) break;
+    float a = 0, b = 0;
+    if (cudaEventElapsedTime(&a, t[0], t[1]) == cudaSuccess && cudaEventElapsedTime(&b, t[1], t[2]) == cudaSuccess)
+      fold_trial(h, a, b);
+    for (cudaEvent_t e : t) h->ev_pool.push_back(e);
+  }
+  h->ev_pending.erase(h->ev_pending.begin(), h->ev_pending.begin() + (long)k);
   cudaGetLastError();
 }
 
@@ -885,6 +923,8 @@ void waves_destroy(waves_handle* h) {
   for (auto& t : h->ev_pending)
     for (cudaEvent_t e : t) h->ev_pool.push_back(e);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  for (auto& sub : h->inflight) cudaEventDestroy(sub.done);
+  if (h->frame_c) cudaFreeHost(h->frame_c);
   for (auto it = h->allocs.rbegin(); it != h->allocs.rend(); ++it) cudaFree(it->ptr);
   if (h->export_planes) cudaFree(h->export_planes);
   if (h->export_kinds) cudaFree(h->export_kinds);
@@ -922,6 +962,67 @@ waves_status waves_advance(waves_handle* h, int32_t max_trials) {
     } else if ((st = host_trial(h)) != WAVES_OK)
       return st;
   }
+  return WAVES_OK;
+}
+
+waves_status waves_frame(waves_handle* h, const waves_frame_budget* budget, waves_frame_report* report) {
+  if (!h || !budget || !report || !(budget->gpu_budget_ms > 0) || budget->max_inflight < 1 ||
+      budget->max_inflight > waves_handle::kFrameSlots || budget->max_trials < 1)
+    return WAVES_INVALID_ARG;
+  cudaSetDevice(h->cfg.device);
+  if (!h->frame_c) CK(cudaMallocHost((void**)&h->frame_c, sizeof(double) * WAVES_CONTROL_SIZE * waves_handle::kFrameSlots));
+  collect_timing_ready(h);
+  // retire finished submissions in order; the latest control block is the telemetry
+  while (!h->inflight.empty() && cudaEventQuery(h->inflight.front().done) == cudaSuccess) {
+    const auto sub = h->inflight.front();
+    std::memcpy(h->last_c, h->frame_c + (size_t)sub.slot * WAVES_CONTROL_SIZE, sizeof(h->last_c));
+    h->have_last = true;
+    cudaEventDestroy(sub.done);
+    h->inflight.erase(h->inflight.begin());
+    h->retired++;
+  }
+  cudaGetLastError();
+  std::memset(report, 0, sizeof(*report));
+  const double* c = h->last_c;
+  const double quota = h->quota.load();
+  // work_scheduler.gd:43-48: stop on failure, on a met quota with no trial pending, and at
+  // max_inflight unfinished submissions
+  const bool halt = h->have_last && halted(c);
+  const bool done = h->have_last && quota_met(c, quota) && !(c[4] > .5) && !(c[7] > .5);
+  int trials = 0;
+  if (!halt && !done && (int)h->inflight.size() < budget->max_inflight) {
+    // work_scheduler.gd:55-69: at least one trial, then while the predicted GPU time stays within
+    // the budget and the enqueue time within cpu_budget_ms (a trial with no measurement yet is
+    // predicted at the whole budget)
+    const double cost = h->trial_cost_ms > 0 ? h->trial_cost_ms : budget->gpu_budget_ms;
+    const auto t0 = std::chrono::steady_clock::now();
+    waves_status st;
+    while (trials < budget->max_trials) {
+      if (trials > 0 && (trials + 1) * cost > budget->gpu_budget_ms) break;
+      if ((st = waves_advance(h, 1)) != WAVES_OK) return st;
+      trials++;
+      const double cpu_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (budget->cpu_budget_ms > 0 && cpu_ms >= budget->cpu_budget_ms) break;
+    }
+    const int slot = (int)(h->serial++ % waves_handle::kFrameSlots);
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaMemcpyAsync(h->frame_c + (size_t)slot * WAVES_CONTROL_SIZE, h->D.c, sizeof(double) * WAVES_CONTROL_SIZE,
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaEventRecord(ev, h->stream));
+    h->inflight.push_back({ev, slot, trials});
+  }
+  report->trials_submitted = trials;
+  report->queue_depth = (int32_t)h->inflight.size();
+  report->idle = done && h->inflight.empty() ? 1 : 0;
+  report->halted = halt ? 1 : 0;
+  report->trial_cost_ms = h->trial_cost_ms;
+  report->predicted_gpu_ms = trials * h->trial_cost_ms;
+  report->gpu_ms_total = h->gpu_ms_total;
+  report->accepted_time = h->have_last ? c[1] : 0.0;
+  report->accepted_steps = h->have_last ? (int64_t)c[2] : 0;
+  report->r_fluid = report->accepted_time > 0 ? h->gpu_ms_total / 1e3 / report->accepted_time : -1.0;
+  report->submissions_retired = h->retired;
   return WAVES_OK;
 }
 
