@@ -195,6 +195,12 @@ waves_status waves_inject_rejection(waves_handle* h);
 /* Accepted-surface export (pressure_pass.glslinc:127-130, op 19): planes[4N] = (normal, alpha)
  * per cell and kinds[N] = 0 air, 1 liquid, 2 mixed, x-fastest.  Host buffers. */
 waves_status waves_export_surface(waves_handle* h, float* planes, float* kinds);
+/* The same export into caller DEVICE buffers (planes 16-byte aligned), enqueued on the handle's
+ * stream without waiting: a headless stand-in for the planes/kinds Texture3DRD.  When clock is not
+ * NULL (16-byte aligned), the same launch writes the surface clock of surface_clock.glsl:1-7 (run
+ * after op 19, coastal_view.gd:19-23): clock[4] = (accepted time, accepted steps, 0, 0) as float,
+ * the committed clock of the exported surface, also after a rejected trial. */
+waves_status waves_export_surface_device(waves_handle* h, void* planes, void* kinds, void* clock);
 
 /* Bank access.  bank = 0/1 physical bank, -1 the accepted bank.  A bank is
  * [F: N][u: (nx+1) ny nz][v: nx (ny+1) nz][w: nx ny (nz+1)][p: N] floats, x-fastest. */
@@ -217,9 +223,10 @@ waves_status waves_load(waves_handle* h, const void* buffer, size_t bytes);
  * folds the GPU times of finished trials into a running per-trial cost (exponential average,
  * weight 0.25, as the reference averages its chunk costs), retires finished submissions (their
  * control block, copied asynchronously, becomes the reported telemetry), and -- unless the solver
- * halted, the quota is met with nothing in flight, or max_inflight submissions are unfinished --
+ * halted, the quota is met with no trial pending, or max_inflight submissions are unfinished --
  * enqueues as many trials as gpu_budget_ms admits at that cost (at least one, at most max_trials,
- * stopping early once enqueueing took cpu_budget_ms) followed by the control-block copy.  It never waits for the GPU and never changes a result. */
+ * stopping early once enqueueing took cpu_budget_ms) followed by the control-block copy.  It
+ * never waits for the GPU and never changes a result. */
 typedef struct waves_frame_budget {
   double gpu_budget_ms;  /* predicted GPU time per frame (reference default 14) */
   int32_t max_inflight;  /* unfinished submissions allowed (reference 3, at most 8) */

@@ -136,3 +136,46 @@ def test_poisoned_fraction_retry_parity(gpu_lib):
     assert cg[33] in (10.0, 11.0, 12.0) or cg[7] in (10.0, 11.0, 12.0)
     problems = compare_state(g, o, cfg, "after poisoned fraction")
     assert not problems, "\n".join(problems)
+
+
+def check_export(g, o):
+    """Host export bit for bit against the oracle's op 19; the device export (caller buffers) equal
+    to the host one, with the surface clock of surface_clock.glsl:7."""
+    import torch
+    planes, kinds = g.export_surface()
+    po, ko = o.export()
+    m = first_mismatch(planes.ravel(), po.ravel())
+    assert not m, f"planes: {m}"
+    assert np.array_equal(kinds, ko)
+    pd = torch.full((g.N, 4), -7.0, dtype=torch.float32, device="cuda")
+    kd = torch.full((g.N,), -7.0, dtype=torch.float32, device="cuda")
+    clock = torch.full((4,), -7.0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    g.export_surface_device(pd.data_ptr(), kd.data_ptr(), clock.data_ptr())
+    g.synchronize()
+    assert np.array_equal(pd.cpu().numpy(), planes) and np.array_equal(kd.cpu().numpy(), kinds)
+    c = g.control()
+    assert clock.cpu().numpy().tolist() == [np.float32(c[1]), np.float32(c[2]), 0.0, 0.0]
+
+
+@pytest.mark.gpu
+def test_surface_export_parity(gpu_lib):
+    """Op 19 export and the surface clock after accepted steps and after a rejected trial (the
+    clock keeps the committed time, coastal_view.gd:19-23)."""
+    cfg = CASES["beach_slope"]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for s in (g, o):
+        s.request_steps(3)
+        s.run()
+    check_export(g, o)
+    g.inject_rejection()
+    c = o.control()
+    c[19] = 1
+    o.set_control(c)
+    for s in (g, o):
+        s.request_steps(4)
+        s.run()
+    assert g.control()[2] == 3 and g.control()[7] == 4
+    check_export(g, o)
+    g.close()

@@ -214,6 +214,16 @@ class WavesSolver:
                                                kinds.ctypes.data_as(C.POINTER(C.c_float))))
         return planes.reshape(-1, 4), kinds
 
+    def export_surface_device(self, planes_ptr, kinds_ptr, clock_ptr=None):
+        """Enqueue the export into caller device buffers (waves_export_surface_device): planes
+        float4[N], kinds float[N], clock float4 (accepted time, accepted steps, 0, 0) or None.
+        Does not wait; order against other streams through `stream()`."""
+        self._ck(self.lib.waves_export_surface_device(self.h, C.c_void_p(planes_ptr), C.c_void_p(kinds_ptr),
+                                                      C.c_void_p(clock_ptr) if clock_ptr else None))
+
+    def stream(self):
+        return self.lib.waves_stream(self.h)
+
     def save(self):
         n = C.c_size_t(0)
         self._ck(self.lib.waves_save(self.h, None, C.byref(n)))

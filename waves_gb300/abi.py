@@ -192,6 +192,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_control",
     "waves_set_control",
     "waves_export_surface",
+    "waves_export_surface_device",
     "waves_bank_floats",
     "waves_get_bank",
     "waves_set_bank",
@@ -231,6 +232,7 @@ def declare(lib):
         "waves_control": (C.c_int, [h, P(C.c_double), C.c_int32]),
         "waves_set_control": (C.c_int, [h, P(C.c_double), C.c_int32]),
         "waves_export_surface": (C.c_int, [h, P(C.c_float), P(C.c_float)]),
+        "waves_export_surface_device": (C.c_int, [h, C.c_void_p, C.c_void_p, C.c_void_p]),
         "waves_bank_floats": (C.c_size_t, [h]),
         "waves_get_bank": (C.c_int, [h, C.c_int32, P(C.c_float)]),
         "waves_set_bank": (C.c_int, [h, C.c_int32, P(C.c_float)]),

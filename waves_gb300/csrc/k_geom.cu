@@ -707,10 +707,14 @@ __global__ void __launch_bounds__(NT) k_coast_momentum(const __grid_constant__ D
 }
 
 // ---------------------------------------------------------------- export (op 19) into buffers
-__global__ void __launch_bounds__(NT) k_export(const __grid_constant__ Dev D, float4* planes, float* kinds) {
+// Op 19 (pressure_pass.glslinc:127-130) and, when `clock` is given, the surface clock of
+// surface_clock.glsl:7: the committed (accepted time, accepted steps) read after the export.
+__global__ void __launch_bounds__(NT) k_export(const __grid_constant__ Dev D, float4* planes, float* kinds,
+                                               float4* clock) {
   grid_dep_wait(D.pdl_early);
   Geo G(D, 19);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
+  if (i == 0 && clock) *clock = make_float4((float)D.c[1], (float)D.c[2], 0.f, 0.f);
   if (i >= D.N) return;
   float f = G.A[i];
   planes[i] = G.reconstruct(G.g.coord(i));
@@ -746,8 +750,8 @@ void launch_post(const Dev& D, cudaStream_t s) {
 }
 void launch_ext_masks(const Dev& D, cudaStream_t s) { pdl_launch(k_ext_masks, grid_for(D.NF), NT, 0, s, D); }
 void launch_trial_end(const Dev& D, cudaStream_t s) { pdl_launch(k_trial_end, 1, NT, 0, s, D); }
-void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds) {
-  pdl_launch(k_export, grid_for(D.N), NT, 0, s, D, planes, kinds);
+void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds, float4* clock) {
+  pdl_launch(k_export, grid_for(D.N), NT, 0, s, D, planes, kinds, clock);
 }
 
 }  // namespace wg

@@ -92,7 +92,7 @@ void launch_proj_setup(const Dev& D, cudaStream_t s);
 void launch_post(const Dev& D, cudaStream_t s);
 void launch_trial_end(const Dev& D, cudaStream_t s);
 void launch_ext_masks(const Dev& D, cudaStream_t s);  // static face neighbourhoods (set-up)
-void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds);
+void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds, float4* clock = nullptr);
 // k_mg.cu
 void launch_mg_build(const Dev& D, cudaStream_t s);
 void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase);

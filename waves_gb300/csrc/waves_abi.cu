@@ -1164,6 +1164,15 @@ waves_status waves_export_surface(waves_handle* h, float* planes, float* kinds) 
   return WAVES_OK;
 }
 
+waves_status waves_export_surface_device(waves_handle* h, void* planes, void* kinds, void* clock) {
+  if (!h || !planes || !kinds || ((uintptr_t)planes & 15) || ((uintptr_t)kinds & 3) || ((uintptr_t)clock & 15))
+    return WAVES_INVALID_ARG;
+  cudaSetDevice(h->cfg.device);
+  wg::launch_export(h->D, h->stream, (float4*)planes, (float*)kinds, (float4*)clock);
+  CK(cudaGetLastError());
+  return WAVES_OK;
+}
+
 size_t waves_bank_floats(const waves_handle* h) { return h ? (size_t)h->D.S : 0; }
 
 waves_status waves_get_bank(waves_handle* h, int32_t bank, float* out) {
