@@ -199,8 +199,27 @@ def run_ours(args, world, rank, local):
         e2e = {"sim_s": sim_e, "wall_s": w, "frames": args.e2e_frames,
                "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8)}
     out["e2e"] = e2e
+    out["render"] = time_render(s, torch)
     s.close()
     return out
+
+
+def time_render(s, torch, width=1280, height=720, frames=10):
+    """Headless presentation: surface export + water ray-march of one 1280x720 frame into device
+    buffers (waves_render_device), CUDA events on the solver's stream, after two warm-up frames."""
+    p = s.render_params(width, height)
+    rgba = torch.empty((height, width, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(s.stream())
+    for _ in range(2):
+        s.render_device(p, rgba.data_ptr())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(frames):
+        s.render_device(p, rgba.data_ptr())
+    b.record(stream)
+    b.synchronize()
+    return {"view": "water", "width": width, "height": height, "ms_per_frame": a.elapsed_time(b) / frames,
+            "launches_per_frame": 2}
 
 
 def measured_peaks():
@@ -330,6 +349,7 @@ def main():
         "trials": res["trials"],
         "clocks": res["clocks"],
         "gpu_launches": res["launches"],
+        "render": res["render"],
     }
     roof, kernels = roofline(res["probes"])
     line["roofline"] = roof

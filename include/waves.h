@@ -202,6 +202,37 @@ waves_status waves_export_surface(waves_handle* h, float* planes, float* kinds);
  * the committed clock of the exported surface, also after a rejected trial. */
 waves_status waves_export_surface_device(waves_handle* h, void* planes, void* kinds, void* clock);
 
+/* Headless presentation (water/presentation/water.gdshader:21-176 with daylight.gdshaderinc,
+ * water/shaders/render/clay.gdshader:8-66): one ray per pixel through the exported PLIC surface,
+ * marched cell by cell, into a float RGBA image (row 0 at the top).  Mode 1 (water) sums the
+ * occupied intervals along the ray, shades with the optical normal, ripples driven by the surface
+ * clock, Fresnel sky reflection, absorption and a specular sun; what the fragment shader reads from
+ * the rendered scene is an analytic scene here (the sky, and the sand bed of presentation.gd:
+ * 94-112 when slope > 0).  Mode 0 (clay) shades the first liquid entry.  The optional trace image
+ * holds per pixel (first entry distance or -1, occupied length, exit of the first interval (clay:
+ * box exit), texture queries). */
+typedef struct waves_render_params {
+  int32_t width, height;
+  int32_t mode;               /* 0 clay, 1 water */
+  int32_t orthographic;       /* 1: `size` is the view height (m); 0: perspective, fov_y_deg */
+  float eye[3], target[3], up[3];
+  float size, fov_y_deg;
+  float water_tint[3];        /* water.gdshader:12 */
+  float attenuation_distance; /* :14, m */
+  float ripple_strength;      /* :15 */
+  float surface_roughness;    /* :16 */
+  float sun_direction[3];     /* daylight.gdshaderinc:2 */
+  int32_t contact_correction; /* :18, with the bed of config slope > 0 */
+  int32_t clock_ready;        /* :19, ripple phase from the surface clock (accepted time) */
+} waves_render_params;
+/* Defaults of water.gdshader and the camera of presentation.gd:83-93 (camera_preset(1),
+ * orthographic, "wide" when nz hz > 1 m) at width x height. */
+void waves_render_params_default(waves_render_params* p, const waves_config* cfg, int32_t width, int32_t height);
+/* Export + render; rgba[4 width height] and trace (NULL or 4 width height) are host buffers. */
+waves_status waves_render(waves_handle* h, const waves_render_params* p, float* rgba, float* trace);
+/* The same into caller device buffers (16-byte aligned), enqueued on the handle's stream. */
+waves_status waves_render_device(waves_handle* h, const waves_render_params* p, void* rgba, void* trace);
+
 /* Bank access.  bank = 0/1 physical bank, -1 the accepted bank.  A bank is
  * [F: N][u: (nx+1) ny nz][v: nx (ny+1) nz][w: nx ny (nz+1)][p: N] floats, x-fastest. */
 size_t waves_bank_floats(const waves_handle* h);

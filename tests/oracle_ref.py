@@ -9,7 +9,7 @@ import subprocess
 
 import numpy as np
 
-from waves_gb300.abi import WavesConfig, WAVES_CONTROL_SIZE
+from waves_gb300.abi import WavesConfig, WavesRenderParams, WAVES_CONTROL_SIZE
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
@@ -47,6 +47,7 @@ def lib():
             "wo_get_masks": (None, [vp, fp, fp]),
             "wo_set_masks": (None, [vp, fp, fp]),
             "wo_get_export": (None, [vp, fp, fp]),
+            "wo_render": (None, [fp, fp, C.POINTER(WavesConfig), C.POINTER(WavesRenderParams), C.c_float, fp, fp]),
             "wo_get_probes": (None, [vp, fp]),
             "wo_mg_levels": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
             "wo_mg_stencil": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
@@ -178,3 +179,16 @@ class Oracle:
         out = (C.c_uint32 * 32)()
         self.L.wo_mg_state(self.h, out)
         return list(out)
+
+
+def render(planes, kinds, cfg, params, clock_time):
+    """The oracle's ray-march of an op-19 export (oracle/wo_render.cpp): (H, W, 4) RGBA and trace."""
+    L = lib()
+    fp = C.POINTER(C.c_float)
+    planes = np.ascontiguousarray(planes, dtype=np.float32)
+    kinds = np.ascontiguousarray(kinds, dtype=np.float32)
+    img = np.empty((params.height, params.width, 4), dtype=np.float32)
+    tr = np.empty_like(img)
+    L.wo_render(planes.ctypes.data_as(fp), kinds.ctypes.data_as(fp), C.byref(cfg), C.byref(params),
+                float(np.float32(clock_time)), img.ctypes.data_as(fp), tr.ctypes.data_as(fp))
+    return img, tr

@@ -140,3 +140,60 @@ def test_injected_rejection_and_retry_paths():
     o2.run()
     c = o2.control()
     assert c[33] in (10.0, 11.0, 12.0) or c[7] in (10.0, 11.0, 12.0)
+
+
+def flat_pool(level=0.43, n=(8, 8, 4), h=0.1):
+    """Op-19 export of still water at y = level over a flat floor (no bed), box from the origin."""
+    from waves_gb300.abi import WavesConfig
+    cfg = WavesConfig()
+    for k in range(3):
+        cfg.n[k], cfg.spacing[k], cfg.origin[k] = n[k], h, 0.0
+    cfg.slope = 0.0
+    nx, ny, nz = n
+    planes = np.zeros((nz, ny, nx, 4), dtype=np.float32)
+    kinds = np.zeros((nz, ny, nx), dtype=np.float32)
+    full = int(level // h)
+    kinds[:, :full, :] = 1.0
+    frac = level / h - full
+    kinds[:, full, :] = 2.0
+    planes[:, full, :] = (0.0, 1.0, 0.0, frac)  # liquid where n . x <= alpha in cell units
+    return cfg, planes.reshape(-1, 4), kinds.ravel()
+
+
+def top_view(mode):
+    from waves_gb300.abi import WavesRenderParams
+    p = WavesRenderParams()
+    p.width, p.height, p.mode, p.orthographic = 16, 16, mode, 1
+    p.eye[:] = (0.4, 2.0, 0.2)
+    p.target[:] = (0.4, 0.0, 0.2)
+    p.up[:] = (0.0, 0.0, -1.0)
+    p.size = 0.6
+    p.water_tint[:] = (0.02745, 0.56078, 0.62353)
+    p.attenuation_distance, p.ripple_strength, p.surface_roughness = 0.18, 0.0025, 0.3
+    p.sun_direction[:] = (-0.45, 0.65, -0.63)
+    p.contact_correction, p.clock_ready = 1, 1
+    return p
+
+
+def test_render_oracle_known_answers():
+    """Straight down through still water (clay.gdshader / water.gdshader): the first entry is the
+    eye height above the surface, the occupied length the water depth, the clay shade the Lambert
+    term of an upward normal; rays outside the box footprint miss."""
+    from tests.oracle_ref import render
+    cfg, planes, kinds = flat_pool()
+    img, tr = render(planes, kinds, cfg, top_view(0), 0.0)
+    hit = tr[..., 0] >= 0
+    # rows sample z = -0.081 + 0.0375 k over the box's [0, 0.4]: rows 3..12 hit
+    assert hit.sum() == 10 * 16 and np.all(hit[3:13]) and np.all(img[~hit] == 0)
+    assert np.allclose(tr[hit, 0], 2.0 - 0.43, atol=2e-6)
+    light = np.array([-0.4, 0.8, 0.5]) / np.linalg.norm([-0.4, 0.8, 0.5])
+    assert np.allclose(img[hit, :3], 0.54 * (0.28 + 0.72 * light[1]), atol=1e-6)
+    assert np.all(img[hit, 3] == 1)
+    img, tr = render(planes, kinds, cfg, top_view(1), 0.0)
+    hit = tr[..., 0] >= 0
+    assert hit.sum() == 10 * 16
+    assert np.allclose(tr[hit, 0], 2.0 - 0.43, atol=2e-6)
+    assert np.allclose(tr[hit, 1], 0.43, atol=2e-6)  # occupied: surface to floor
+    assert np.allclose(tr[hit, 2], 2.0, atol=2e-6)  # one interval, leaving through the floor
+    # deeper water is darker in red (absorption 1.4 / 0.18 per metre) than the sky behind a miss
+    assert np.all(img[hit, 0] < img[~hit, 0].min())

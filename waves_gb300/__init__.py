@@ -221,6 +221,34 @@ class WavesSolver:
         self._ck(self.lib.waves_export_surface_device(self.h, C.c_void_p(planes_ptr), C.c_void_p(kinds_ptr),
                                                       C.c_void_p(clock_ptr) if clock_ptr else None))
 
+    def render_params(self, width=1280, height=720, **overrides):
+        """waves_render_params_default for this configuration, with field overrides."""
+        from .abi import WavesRenderParams
+        p = WavesRenderParams()
+        self.lib.waves_render_params_default(C.byref(p), C.byref(self.cfg), int(width), int(height))
+        for k, v in overrides.items():
+            field = getattr(p, k)
+            if hasattr(field, "__len__"):
+                for i, x in enumerate(v):
+                    field[i] = x
+            else:
+                setattr(p, k, v)
+        return p
+
+    def render(self, params=None, trace=False):
+        """Export + ray-march (waves_render): an (H, W, 4) float32 RGBA image, and with trace=True
+        also the (H, W, 4) trace image (first entry, occupied length, first exit, queries)."""
+        p = params if params is not None else self.render_params()
+        img = np.empty((p.height, p.width, 4), dtype=np.float32)
+        tr = np.empty((p.height, p.width, 4), dtype=np.float32) if trace else None
+        self._ck(self.lib.waves_render(self.h, C.byref(p), img.ctypes.data_as(C.POINTER(C.c_float)),
+                                       tr.ctypes.data_as(C.POINTER(C.c_float)) if trace else None))
+        return (img, tr) if trace else img
+
+    def render_device(self, params, rgba_ptr, trace_ptr=None):
+        self._ck(self.lib.waves_render_device(self.h, C.byref(params), C.c_void_p(rgba_ptr),
+                                              C.c_void_p(trace_ptr) if trace_ptr else None))
+
     def stream(self):
         return self.lib.waves_stream(self.h)
 

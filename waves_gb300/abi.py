@@ -131,6 +131,27 @@ class WavesWarmStartModel(C.Structure):
     ]
 
 
+class WavesRenderParams(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("mode", C.c_int32),
+        ("orthographic", C.c_int32),
+        ("eye", C.c_float * 3),
+        ("target", C.c_float * 3),
+        ("up", C.c_float * 3),
+        ("size", C.c_float),
+        ("fov_y_deg", C.c_float),
+        ("water_tint", C.c_float * 3),
+        ("attenuation_distance", C.c_float),
+        ("ripple_strength", C.c_float),
+        ("surface_roughness", C.c_float),
+        ("sun_direction", C.c_float * 3),
+        ("contact_correction", C.c_int32),
+        ("clock_ready", C.c_int32),
+    ]
+
+
 class WavesFrameBudget(C.Structure):
     _fields_ = [
         ("gpu_budget_ms", C.c_double),
@@ -193,6 +214,9 @@ WAVES_ABI_SYMBOLS = [
     "waves_set_control",
     "waves_export_surface",
     "waves_export_surface_device",
+    "waves_render_params_default",
+    "waves_render",
+    "waves_render_device",
     "waves_bank_floats",
     "waves_get_bank",
     "waves_set_bank",
@@ -233,6 +257,9 @@ def declare(lib):
         "waves_set_control": (C.c_int, [h, P(C.c_double), C.c_int32]),
         "waves_export_surface": (C.c_int, [h, P(C.c_float), P(C.c_float)]),
         "waves_export_surface_device": (C.c_int, [h, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "waves_render_params_default": (None, [P(WavesRenderParams), cfgp, C.c_int32, C.c_int32]),
+        "waves_render": (C.c_int, [h, P(WavesRenderParams), P(C.c_float), P(C.c_float)]),
+        "waves_render_device": (C.c_int, [h, P(WavesRenderParams), C.c_void_p, C.c_void_p]),
         "waves_bank_floats": (C.c_size_t, [h]),
         "waves_get_bank": (C.c_int, [h, C.c_int32, P(C.c_float)]),
         "waves_set_bank": (C.c_int, [h, C.c_int32, P(C.c_float)]),

@@ -17,7 +17,7 @@ LIB = os.path.join(OUT, "libwaves_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["waves_abi.cu", "k_pcg.cu", "k_motion.cu", "k_geom.cu", "k_mg.cu", "k_init.cu", "k_net.cu", "noalloc.cu", "config.cpp"]
+SOURCES = ["waves_abi.cu", "k_pcg.cu", "k_motion.cu", "k_geom.cu", "k_mg.cu", "k_init.cu", "k_net.cu", "k_render.cu", "noalloc.cu", "config.cpp"]
 
 
 def nvcc():
@@ -80,7 +80,7 @@ def build_harness():
     cuda = os.path.dirname(os.path.dirname(nvcc()))
     cmd = [cc, "-std=c11", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"),
            os.path.join(HERE, "harness", "waves_run.c"), "-o", HARNESS, "-L", OUT, "-lwaves_gb300",
-           "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+           "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64"), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness build failed:\n{r.stdout}\n{r.stderr}")

@@ -93,6 +93,21 @@ void launch_post(const Dev& D, cudaStream_t s);
 void launch_trial_end(const Dev& D, cudaStream_t s);
 void launch_ext_masks(const Dev& D, cudaStream_t s);  // static face neighbourhoods (set-up)
 void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds, float4* clock = nullptr);
+// k_render.cu: headless presentation of the exported surface
+struct RenderArgs {
+  const float4* planes;
+  const float* kinds;
+  const double* c;  // control block (surface clock c[1])
+  float4* rgba;
+  float4* trace;  // optional: first entry, occupied length, first-interval exit (clay: box exit), queries
+  int nx, ny, nz, width, height;
+  int mode;  // 0 clay, 1 water
+  int ortho, contact, clock_ready;
+  float bmin[3], bmax[3], slope;
+  float eye[3], fwd[3], right[3], up[3], half_w, half_h;
+  float tint[3], attenuation, ripple, roughness, sun[3];
+};
+void launch_render(const RenderArgs& A, cudaStream_t s);
 // k_mg.cu
 void launch_mg_build(const Dev& D, cudaStream_t s);
 void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase);

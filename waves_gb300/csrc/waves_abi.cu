@@ -63,6 +63,8 @@ struct waves_handle {
   float4* probes = nullptr;
   float4* export_planes = nullptr;
   float* export_kinds = nullptr;
+  float4* render_buf = nullptr;  // waves_render: image and trace
+  size_t render_px = 0;
   double* host_c = nullptr;  // pinned
   double* host_quota = nullptr;  // pinned
   std::atomic<double> quota{0.0};
@@ -928,6 +930,7 @@ void waves_destroy(waves_handle* h) {
   for (auto it = h->allocs.rbegin(); it != h->allocs.rend(); ++it) cudaFree(it->ptr);
   if (h->export_planes) cudaFree(h->export_planes);
   if (h->export_kinds) cudaFree(h->export_kinds);
+  if (h->render_buf) cudaFree(h->render_buf);
   if (h->host_c) cudaFreeHost(h->host_c);
   if (h->host_quota) cudaFreeHost(h->host_quota);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1170,6 +1173,130 @@ waves_status waves_export_surface_device(waves_handle* h, void* planes, void* ki
   cudaSetDevice(h->cfg.device);
   wg::launch_export(h->D, h->stream, (float4*)planes, (float*)kinds, (float4*)clock);
   CK(cudaGetLastError());
+  return WAVES_OK;
+}
+
+void waves_render_params_default(waves_render_params* p, const waves_config* cfg, int32_t width, int32_t height) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->width = width;
+  p->height = height;
+  p->mode = 1;
+  p->orthographic = 1;
+  // camera_preset(1) of presentation.gd:86-93
+  const bool wide = cfg && (double)cfg->n[2] * cfg->spacing[2] > 1.0;
+  const float tg[3] = {wide ? 2.15f : 3.45f, wide ? -0.12f : -0.08f, 0.f};
+  const float off[3] = {wide ? 2.5f : 1.5f, wide ? 4.45f : 2.f, wide ? 5.7f : 3.f};
+  for (int k = 0; k < 3; k++) {
+    p->target[k] = tg[k];
+    p->eye[k] = tg[k] + off[k];
+  }
+  p->up[1] = 1.f;
+  p->size = wide ? 5.25f : 1.5f;
+  p->fov_y_deg = 75.f;
+  p->water_tint[0] = 0.02745f;
+  p->water_tint[1] = 0.56078f;
+  p->water_tint[2] = 0.62353f;
+  p->attenuation_distance = 0.18f;
+  p->ripple_strength = 0.0025f;
+  p->surface_roughness = 0.30f;
+  p->sun_direction[0] = -0.45f;
+  p->sun_direction[1] = 0.65f;
+  p->sun_direction[2] = -0.63f;
+  p->contact_correction = 1;
+  p->clock_ready = 1;
+}
+
+namespace {
+// Camera basis in FP32 (forward, right = forward x up, up' = right x forward, all normalised
+// except up'), with the image half-extents at unit distance (perspective) or in metres
+// (orthographic).
+bool render_args(waves_handle* h, const waves_render_params* p, wg::RenderArgs& A) {
+  if (!p || p->width < 1 || p->height < 1 || p->width > 16384 || p->height > 16384 || (p->mode != 0 && p->mode != 1))
+    return false;
+  if (p->orthographic ? !(p->size > 0.f) : !(p->fov_y_deg > 0.f && p->fov_y_deg < 179.f)) return false;
+  auto nrm = [](float v[3]) {
+    const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (!(l > 0.f)) return false;
+    for (int k = 0; k < 3; k++) v[k] = v[k] / l;
+    return true;
+  };
+  std::memset(&A, 0, sizeof(A));
+  float f[3] = {p->target[0] - p->eye[0], p->target[1] - p->eye[1], p->target[2] - p->eye[2]};
+  if (!nrm(f)) return false;
+  float r[3] = {f[1] * p->up[2] - f[2] * p->up[1], f[2] * p->up[0] - f[0] * p->up[2], f[0] * p->up[1] - f[1] * p->up[0]};
+  if (!nrm(r)) return false;
+  const float u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+  for (int k = 0; k < 3; k++) {
+    A.eye[k] = p->eye[k];
+    A.fwd[k] = f[k];
+    A.right[k] = r[k];
+    A.up[k] = u[k];
+    A.bmin[k] = h->cfg.origin[k];
+    A.bmax[k] = h->cfg.origin[k] + (float)h->cfg.n[k] * h->cfg.spacing[k];
+    A.tint[k] = p->water_tint[k];
+    A.sun[k] = p->sun_direction[k];
+  }
+  A.half_h = p->orthographic ? p->size * 0.5f : (float)std::tan((double)p->fov_y_deg * M_PI / 360.0);
+  A.half_w = A.half_h * ((float)p->width / (float)p->height);
+  A.nx = h->cfg.n[0];
+  A.ny = h->cfg.n[1];
+  A.nz = h->cfg.n[2];
+  A.width = p->width;
+  A.height = p->height;
+  A.mode = p->mode;
+  A.ortho = p->orthographic ? 1 : 0;
+  A.contact = p->contact_correction ? 1 : 0;
+  A.clock_ready = p->clock_ready ? 1 : 0;
+  A.slope = h->cfg.slope;
+  A.attenuation = p->attenuation_distance;
+  A.ripple = p->ripple_strength;
+  A.roughness = p->surface_roughness;
+  A.c = h->D.c;
+  return true;
+}
+waves_status render_enqueue(waves_handle* h, wg::RenderArgs& A) {
+  if (!h->export_planes) {
+    CK(cudaMalloc(&h->export_planes, (size_t)h->D.N * sizeof(float4)));
+    CK(cudaMalloc(&h->export_kinds, (size_t)h->D.N * sizeof(float)));
+  }
+  wg::launch_export(h->D, h->stream, h->export_planes, h->export_kinds);
+  A.planes = h->export_planes;
+  A.kinds = h->export_kinds;
+  wg::launch_render(A, h->stream);
+  CK(cudaGetLastError());
+  return WAVES_OK;
+}
+}  // namespace
+
+waves_status waves_render_device(waves_handle* h, const waves_render_params* p, void* rgba, void* trace) {
+  wg::RenderArgs A;
+  if (!h || !rgba || ((uintptr_t)rgba & 15) || ((uintptr_t)trace & 15) || !render_args(h, p, A)) return WAVES_INVALID_ARG;
+  cudaSetDevice(h->cfg.device);
+  A.rgba = (float4*)rgba;
+  A.trace = (float4*)trace;
+  return render_enqueue(h, A);
+}
+
+waves_status waves_render(waves_handle* h, const waves_render_params* p, float* rgba, float* trace) {
+  wg::RenderArgs A;
+  if (!h || !rgba || !render_args(h, p, A)) return WAVES_INVALID_ARG;
+  cudaSetDevice(h->cfg.device);
+  const size_t px = (size_t)p->width * p->height;
+  if (h->render_px < px) {
+    if (h->render_buf) cudaFree(h->render_buf);
+    h->render_buf = nullptr;
+    h->render_px = 0;
+    CK(cudaMalloc(&h->render_buf, px * 2 * sizeof(float4)));
+    h->render_px = px;
+  }
+  A.rgba = h->render_buf;
+  A.trace = trace ? h->render_buf + px : nullptr;
+  waves_status st;
+  if ((st = render_enqueue(h, A)) != WAVES_OK) return st;
+  CK(cudaMemcpyAsync(rgba, A.rgba, px * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+  if (trace) CK(cudaMemcpyAsync(trace, A.trace, px * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return WAVES_OK;
 }
 

@@ -2,16 +2,19 @@
  * waves_run: headless driver of the waves solver step through the C ABI only (include/waves.h).
  *
  *   waves_run [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16]
- *             [--frame DT] [--surface FILE]
+ *             [--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]
  *
  * It plays the role of the reference's lab runner (water/lab_runner.gd:49-73): it requests
  * accepted time frame by frame (1/60 s by default, request_time), runs the solver until each
  * frame's quota is met, and prints one JSON line per run with the telemetry of waves_stats and
  * the device time of waves_timing.  --surface writes the last accepted surface export (float4
- * planes then float kinds, ops 19/14) to a file.  The exit status is 0 on success, 1 on a bad
+ * planes then float kinds, ops 19/14) to a file; --image renders the last accepted surface
+ * (waves_render, the default camera of the configuration) to a binary PPM, sRGB-encoded.  The
+ * exit status is 0 on success, 1 on a bad
  * argument, 2 when the library fails, 3 when the solver halts.
  */
 #define _POSIX_C_SOURCE 199309L
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -28,6 +31,8 @@ static double now_s(void) {
 int main(int argc, char** argv) {
   const char* preset = "beach";
   const char* surface = NULL;
+  const char* image = NULL;
+  int view = 1, width = 1280, height = 720;
   double seconds = 1.0, frame = 1.0 / 60.0, tol = 1e-6;
   long steps = 0;
   int mg = 32;
@@ -41,9 +46,12 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "--mg") && v) mg = atoi(v), i++;
     else if (!strcmp(a, "--frame") && v) frame = atof(v), i++;
     else if (!strcmp(a, "--surface") && v) surface = v, i++;
+    else if (!strcmp(a, "--image") && v) image = v, i++;
+    else if (!strcmp(a, "--view") && v && (!strcmp(v, "water") || !strcmp(v, "clay"))) view = !strcmp(v, "water"), i++;
+    else if (!strcmp(a, "--size") && v && sscanf(v, "%dx%d", &width, &height) == 2 && width > 0 && height > 0) i++;
     else {
       fprintf(stderr, "usage: %s [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16] "
-                      "[--frame DT] [--surface FILE]\n", argv[0]);
+                      "[--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]\n", argv[0]);
       return 1;
     }
   }
@@ -105,6 +113,30 @@ int main(int argc, char** argv) {
     if (f) fclose(f);
     free(planes);
     free(kinds);
+  }
+  if (image) {
+    waves_render_params p;
+    waves_render_params_default(&p, &cfg, width, height);
+    p.mode = view;
+    const size_t px = (size_t)width * height;
+    float* rgba = (float*)malloc(px * 4 * sizeof(float));
+    unsigned char* rgb = (unsigned char*)malloc(px * 3);
+    FILE* f = rgba && rgb ? fopen(image, "wb") : NULL;
+    if (f && waves_render(h, &p, rgba, NULL) == WAVES_OK) {
+      for (size_t i = 0; i < px; i++)
+        for (int k = 0; k < 3; k++) {
+          double c = rgba[4 * i + k];
+          c = c <= 0.0 ? 0.0 : (c >= 1.0 ? 1.0 : c);
+          rgb[3 * i + k] = (unsigned char)(255.0 * pow(c, 1.0 / 2.2) + 0.5);
+        }
+      fprintf(f, "P6\n%d %d\n255\n", width, height);
+      fwrite(rgb, 1, px * 3, f);
+    } else {
+      fprintf(stderr, "render failed: %s\n", waves_last_error(h));
+    }
+    if (f) fclose(f);
+    free(rgba);
+    free(rgb);
   }
   waves_destroy(h);
   return halted ? 3 : 0;
