@@ -58,6 +58,7 @@ struct MG {
   template <class T> DI T* field(int f, int l) const { return (T*)D.mgv + (long long)f * D.mg_nodes + D.lv[l].off; }
   template <class T> DI bool active(int l, int i) const { return i >= 0 && ld_val(field<T>(3, l)[i]) > .5f; }
   DI float fine_coef(int f, int i) const { return D.snapshot[(long long)(f - 6) * D.N + i]; }
+  DI const float* coarse_inverse() const { return D.mglinv; }
   // coefficient (pressure_multigrid.glslinc:74-88), build-time values from the FP32 rows
   template <class T> DI float coefficient(int l, int i, int j) const {
     if (j < 0) return 0.f;
@@ -129,6 +130,28 @@ struct MG {
         size++;
       }
     }
+    return size;
+  }
+  // transfers() with every table load issued before the first weight is tested, for the
+  // prolongation (the Galerkin build keeps transfers(): there the tests save most loads)
+  DI int transfers_prefetched(int l, int i, int* ids, float* ws) const {
+    const MGLevelDev& lv = D.lv[l];
+    float w[8];
+    int id[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (k < lv.twidth) {
+        w[k] = D.mgtw[lv.toff + (long long)k * lv.count + i];
+        id[k] = D.mgtid[lv.toff + (long long)k * lv.count + i];
+      }
+    int size = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (k < lv.twidth && w[k] > 0.f) {
+        ids[size] = id[k];
+        ws[size] = w[k];
+        size++;
+      }
     return size;
   }
   // apply (pressure_multigrid.glslinc:90-105) with the V-cycle operators; `lin_s` (optional) is a
@@ -651,7 +674,7 @@ template <class T, class M> DI void prolong_cell(const M& m, int l, int ff, int 
     float ws[8];
     // The stored transfers are compute_transfers() on the current coarse mask (rebuilt whenever
     // that mask changes); at level 0 recomputing them is cheaper than reading the table.
-    int size = l == 0 ? m.template compute_transfers<T>(l, i, ids, ws) : m.transfers(l, i, ids, ws);
+    int size = l == 0 ? m.template compute_transfers<T>(l, i, ids, ws) : m.transfers_prefetched(l, i, ids, ws);
     const T* xc = m.template field<T>(cf, l + 1);
     for (int k = 0; k < size; k++) add += ws[k] * ld_val(xc[ids[k]]);
   }
@@ -663,15 +686,16 @@ template <class T, class M> DI void coarse_block(const M& m, int l, float* small
   const Dev& D = m.D;
   const int n = D.lv[l].count, t = threadIdx.x;
   const T* b = m.template field<T>(0, l);
+  const float* linv = m.coarse_inverse();
   if (t < n) {
     float d = 0.f;
-    for (int j = 0; j <= t; j++) d += D.mglinv[t * n + j] * ld_val(b[j]);
+    for (int j = 0; j <= t; j++) d += linv[t * n + j] * ld_val(b[j]);
     small[t] = d;
   }
   __syncthreads();
   if (t < n) {
     float d = 0.f;
-    for (int j = t; j < n; j++) d += D.mglinv[j * n + t] * small[j];
+    for (int j = t; j < n; j++) d += linv[j * n + t] * small[j];
     m.template field<T>(1, l)[t] = st_val<T>(d);
   }
   __syncthreads();
@@ -857,10 +881,12 @@ struct MGs : MG {
   void* vec;
   const void* ell;
   const unsigned short* cols;  // the cached columns max(wrap(q + offset), 0) of the staged rows
+  const float* linv;           // the staged factor of the dense coarse solve
   int base_off, span;
   long long base_eoff;
-  DI MGs(const Dev& d, void* v, const void* e, const unsigned short* c, int lb, int sp)
-      : MG(d), vec(v), ell(e), cols(c), base_off(d.lv[lb].off), span(sp), base_eoff(d.lv[lb].eoff) {}
+  DI MGs(const Dev& d, void* v, const void* e, const unsigned short* c, const float* li, int lb, int sp)
+      : MG(d), vec(v), ell(e), cols(c), linv(li), base_off(d.lv[lb].off), span(sp), base_eoff(d.lv[lb].eoff) {}
+  DI const float* coarse_inverse() const { return linv; }
   template <class T> DI T* field(int f, int l) const { return (T*)vec + f * span + (D.lv[l].off - base_off); }
   template <class T> DI bool active(int l, int i) const { return i >= 0 && ld_val(field<T>(3, l)[i]) > .5f; }
   template <class T> DI float apply(int l, int f, int i, const int* = nullptr) const {
@@ -936,6 +962,11 @@ template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* st
   T* vec = (T*)stage;
   T* ell = (T*)(stage + (((size_t)8 * span * sizeof(T) + 15) & ~(size_t)15));
   unsigned short* cols = (unsigned short*)((unsigned char*)ell + (((size_t)(e1 - e0) * sizeof(T) + 15) & ~(size_t)15));
+  // the dense coarse solve's factor (at most 64 x 64) after the columns
+  const int nc = D.lv[L - 1].count;
+  float* linv = (float*)((unsigned char*)cols + (((size_t)(e1 - e0) * 2 + 15) & ~(size_t)15));
+  if (nc <= 64)
+    for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) linv[k] = D.mglinv[k];
   const T* gvec = (const T*)D.mgv + D.lv[lb].off;
   for (int f = 0; f < 8; f++)
     for (int k = threadIdx.x; k < span; k += blockDim.x) vec[f * span + k] = gvec[(size_t)f * D.mg_nodes + k];
@@ -946,7 +977,7 @@ template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* st
     cols[k] = (unsigned short)gcol[k];
   }
   __syncthreads();
-  bottom_cycle<T>(D, MGs(D, vec, ell, cols, lb, span), lb, small);
+  bottom_cycle<T>(D, MGs(D, vec, ell, cols, nc <= 64 ? linv : D.mglinv, lb, span), lb, small);
   T* out = (T*)D.mgv + D.lv[lb].off;
   for (int f = 0; f < 8; f++)
     for (int k = threadIdx.x; k < span; k += blockDim.x) out[(size_t)f * D.mg_nodes + k] = vec[f * span + k];

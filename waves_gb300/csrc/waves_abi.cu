@@ -540,7 +540,9 @@ waves_status setup_device(waves_handle* h) {
     const int lb = D.mg_bottom, Lc = D.L - 1;
     const size_t span = (size_t)D.lv[Lc].off + D.lv[Lc].count - D.lv[lb].off;
     const size_t rows = (size_t)(D.lv[Lc].eoff + (long long)D.lv[Lc].stencil * D.lv[Lc].count - D.lv[lb].eoff);
-    const size_t bytes = ((8 * span * tsz + 15) & ~(size_t)15) + ((rows * tsz + 15) & ~(size_t)15) + rows * 2;
+    const size_t nc = (size_t)D.lv[Lc].count;
+    const size_t bytes = ((8 * span * tsz + 15) & ~(size_t)15) + ((rows * tsz + 15) & ~(size_t)15) +
+                         ((rows * 2 + 15) & ~(size_t)15) + (nc <= 64 ? nc * nc * sizeof(float) : 0);
     bool narrow = true;  // every staged level indexable in 16 bits
     for (int l = lb; l <= Lc; l++) narrow = narrow && D.lv[l].count <= 65536;
     D.mg_bottom_smem = lb >= 1 && narrow && bytes <= (size_t)wg::kBottomSmemMax ? (int)bytes : 0;
