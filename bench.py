@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--mg", type=int, default=32, choices=[32, 16])
     ap.add_argument("--grid", default="beach", choices=["beach", "large"],
                     help="beach: 310x48x80 (the metric's grid); large: 620x96x160, spacing halved")
-    ap.add_argument("--e2e-frames", type=int, default=30)
+    ap.add_argument("--e2e-frames", type=int, default=-1,
+                    help="1/60 s frames of the end-to-end run; -1: the timed window's simulated span, 0: none")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     return ap.parse_args()
@@ -145,6 +146,7 @@ def run_ours(args, world, rank, local):
     timing(True)
     c0 = s.control()
     stats0 = s.stats()
+    start_state = s.save() if args.e2e_frames != 0 else None
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -182,21 +184,26 @@ def run_ours(args, world, rank, local):
         "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
         "probes": probes if probe_trials else [],
     }
-    # e2e: frames through the public API with host buffers
+    # e2e: frames through the public API with host buffers, from the state the timed steps started
+    # from (checkpoint restored), over the same simulated window unless --e2e-frames says otherwise
     e2e = None
-    if args.e2e_frames > 0:
-        planes = np.empty(4 * s.N, dtype=np.float32)
-        kinds = np.empty(s.N, dtype=np.float32)
+    if args.e2e_frames != 0:
+        s.load(start_state)
+        frames = args.e2e_frames if args.e2e_frames > 0 else max(1, int(round(sim * 60.0)))
+        # page-locked host buffers for the per-frame surface export, as a renderer that reads the
+        # surface every frame would hold them
+        planes = torch.empty(4 * s.N, dtype=torch.float32, pin_memory=True).numpy()
+        kinds = torch.empty(s.N, dtype=torch.float32, pin_memory=True).numpy()
         t_sim0 = s.control()[1]
         w0 = time.perf_counter()
-        for f in range(args.e2e_frames):
+        for f in range(frames):
             s.request_time(t_sim0 + (f + 1) / 60.0)
             s.run(4)
             st = s.stats()
             lib.waves_export_surface(h, planes.ctypes.data_as(C.POINTER(C.c_float)), kinds.ctypes.data_as(C.POINTER(C.c_float)))
         w = time.perf_counter() - w0
         sim_e = s.control()[1] - t_sim0
-        e2e = {"sim_s": sim_e, "wall_s": w, "frames": args.e2e_frames,
+        e2e = {"sim_s": sim_e, "wall_s": w, "frames": frames,
                "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8)}
     out["e2e"] = e2e
     out["render"] = time_render(s, torch)
@@ -363,7 +370,8 @@ def main():
     if res["e2e"]:
         e = res["e2e"]
         line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
-                       "d2h_bytes_per_step": e["d2h"], "step": "one 1/60 s frame: request_time, run, stats, surface export"}
+                       "d2h_bytes_per_step": e["d2h"], "step": "one 1/60 s frame: request_time, run, stats, surface export",
+                       "frames": e["frames"], "window": "the timed steps' simulated span, from their starting state"}
     if world == 1 and not args.no_cpu_baseline:
         try:
             base = cpu_baseline(args, args.mg, args.cpu_seconds)
