@@ -138,6 +138,7 @@ struct Dev {
   void* mgell;               // ELL values [k][i] of levels >= 1 (float or bf16)
   int* mgtid;                // transfer cache ids
   float* mgtw;               // transfer cache weights
+  unsigned long long* mgtq;  // transfer cache: coarse cell coordinates, 21 bits per axis
   float* mglinv;             // dense L^-1 of the last level
   float* snapshot;           // 9 N hierarchy snapshot
   float* previous;           // 9 N previous-trial audit copy

@@ -51,6 +51,28 @@ struct MG {
     return d;
   }
   DI static int slot(I3 d) { return d.x + 2 + 5 * (d.y + 2 + 5 * (d.z + 2)); }
+  // cell coordinates packed 21 bits per axis (the transfer table's coarse coordinates)
+  DI static unsigned long long pack(I3 q) {
+    return (unsigned long long)q.x | ((unsigned long long)q.y << 21) | ((unsigned long long)q.z << 42);
+  }
+  DI static I3 unpack(unsigned long long v) {
+    return mk(int(v & 0x1fffffull), int((v >> 21) & 0x1fffffull), int(v >> 42));
+  }
+  // wrap() on coordinates: false where wrap() returns -1, else q wrapped in place
+  DI bool wrap_q(int l, I3& q) const {
+    const MGLevelDev& v = D.lv[l];
+    q.z = pmod(q.z, v.nz);
+    if (D.px) q.x = pmod(q.x, v.nx);
+    return !(q.x < 0 || q.x >= v.nx || q.y < 0 || q.y >= v.ny);
+  }
+  // delta() from the coordinates of i (qi) and j (qj)
+  DI I3 delta_q(int l, I3 qi, I3 qj) const {
+    const MGLevelDev& v = D.lv[l];
+    I3 d = subI(qj, qi);
+    if (D.px) d.x = pmod(d.x + v.nx / 2, v.nx) - v.nx / 2;
+    d.z = pmod(d.z + v.nz / 2, v.nz) - v.nz / 2;
+    return d;
+  }
   DI I3 offset(int l, int k) const {
     const int* s = D.stencil_tab + 3 * (D.lv[l].soff + k);
     return mk(__ldg(s), __ldg(s + 1), __ldg(s + 2));
@@ -393,6 +415,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __g
   for (int k = 0; k < lv.twidth; k++) {
     D.mgtid[lv.toff + (long long)k * lv.count + i] = k < size ? ids[k] : 0;
     D.mgtw[lv.toff + (long long)k * lv.count + i] = k < size ? ws[k] : 0.f;
+    D.mgtq[lv.toff + (long long)k * lv.count + i] = k < size ? MG::pack(m.coord(l + 1, ids[k])) : 0ull;
   }
 }
 // l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
@@ -444,7 +467,10 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
   const MGLevelDev& fl = D.lv[l];
   const MGLevelDev& cl = D.lv[l + 1];
   const int t = threadIdx.x;
+  __shared__ I3 offs[kMaxStencil];
+  for (int k = t; k < fl.stencil; k += GT) offs[k] = m.offset(l, k);
   for (int s = 0; s < 125; s++) part[s * GT + t] = 0.f;
+  __syncthreads();
   int row_local = t / G, g = t % G;
   int I = blockIdx.x * rpb + row_local;
   if (row_local < rpb && I < cl.count && m.active<T>(l + 1, I)) {
@@ -452,31 +478,64 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
     int lo[3], ext[3];
     for (int a = 0; a < 3; a++) child_range(D, l, a, qc[a], lo[a], ext[a]);
     int gz = g / ey, gy = g % ey;
+    // Cell coordinates are carried along instead of decoded from indices: qi from the loop, qj
+    // from qi + offset, and the coarse coordinates of j's transfers from the table (mgtq).  The
+    // terms and their order are those of the index form: for each fine cell i (x fastest in this
+    // thread's row of children), each of i's transfers to I, each stencil neighbour j, each of j's
+    // transfers.
+    const long long tstride = fl.count;
     for (int gx = 0; gx < ext[0]; gx++) {
-      int i = m.wrap(l, mk(lo[0] + gx, lo[1] + gy, lo[2] + gz));
-      if (i < 0 || !m.active<T>(l, i)) continue;
-      int li[8], ri[8];
-      float lw[8], rw[8];
+      I3 qi = mk(lo[0] + gx, lo[1] + gy, lo[2] + gz);
+      if (!m.wrap_q(l, qi)) continue;
+      const int i = qi.x + fl.nx * (qi.y + fl.ny * qi.z);
+      if (!m.active<T>(l, i)) continue;
+      int li[8];
+      float lw[8];
       int nl = m.transfers(l, i, li, lw);
-      I3 qi = m.coord(l, i);
       for (int a = 0; a < nl; a++) {
         if (li[a] != I) continue;
         for (int k = 0; k < fl.stencil; k++) {
-          I3 off = m.offset(l, k);
-          int j = m.wrap(l, addI(qi, off));
-          if (j < 0 || !m.active<T>(l, j)) continue;
-          if (l > 0 && !m.unique_neighbor(l, i, off, j)) continue;
-          float aij = l == 0 ? (k == 0 ? m.fine_coef(12, i) : -m.fine_coef(5 + k, i)) : m.coefficient<T>(l, i, j);
+          // every load of one neighbour (its activity, the coefficient, its transfers) is issued
+          // before the first test; a neighbour outside the grid loads from i instead
+          const I3 off = offs[k];
+          I3 qj = addI(qi, off);
+          const bool in = m.wrap_q(l, qj);
+          const int j = in ? qj.x + fl.nx * (qj.y + fl.ny * qj.z) : i;
+          if (!in) qj = qi;
+          bool uniq = true;
+          long long maddr = -1;
+          if (l > 0) {
+            // unique_neighbor and coefficient() of two active cells
+            uniq = eqI(m.delta_q(l, qi, qj), off);
+            const bool ilo = i <= j;
+            const I3 d = ilo ? m.delta_q(l, qi, qj) : m.delta_q(l, qj, qi);
+            if (!(abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2)) maddr = fl.moff + (long long)(ilo ? i : j) * 125 + MG::slot(d);
+          }
+          const bool actj = m.active<T>(l, j);
+          const float coef = l == 0 ? (k == 0 ? m.fine_coef(12, i) : -m.fine_coef(5 + k, i)) : (maddr >= 0 ? D.mgmat[maddr] : 0.f);
+          const long long tj = fl.toff + j;
+          float wv[8];
+          unsigned long long qv[8];
+#pragma unroll
+          for (int b = 0; b < 8; b++)
+            if (b < fl.twidth) {
+              wv[b] = D.mgtw[tj + b * tstride];
+              qv[b] = D.mgtq[tj + b * tstride];
+            }
+          if (!in || !actj) continue;
+          if (!uniq) continue;
+          const float aij = coef;
           if (aij == 0.f) continue;
-          int nr = m.transfers(l, j, ri, rw);
-          float al = aij * lw[a];
-          for (int b = 0; b < nr; b++) {
-            I3 d = m.delta(l + 1, I, ri[b]);
+          const float al = aij * lw[a];
+#pragma unroll
+          for (int b = 0; b < 8; b++) {
+            if (b >= fl.twidth || !(wv[b] > 0.f)) continue;
+            const I3 d = m.delta_q(l + 1, qc, MG::unpack(qv[b]));
             if (abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2) {
               D.c[7] = 31;
               continue;
             }
-            part[MG::slot(d) * GT + t] += al * rw[b];
+            part[MG::slot(d) * GT + t] += al * wv[b];
           }
         }
       }

@@ -576,6 +576,7 @@ waves_status setup_device(waves_handle* h) {
   }
   AL(D.mgtid, toff, true, "mg_transfer_ids");
   AL(D.mgtw, toff, true, "mg_transfer_weights");
+  AL(D.mgtq, toff, true, "mg_transfer_coarse_coordinates");
   AL(D.mglinv, 64 * 64, true, "mg_linv");
   AL(D.snapshot, 9 * N, true, "mg_snapshot");
   AL(D.previous, 9 * N, true, "mg_previous");
