@@ -473,70 +473,77 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
   __syncthreads();
   int row_local = t / G, g = t % G;
   int I = blockIdx.x * rpb + row_local;
-  if (row_local < rpb && I < cl.count && m.active<T>(l + 1, I)) {
-    I3 qc = m.coord(l + 1, I);
-    int lo[3], ext[3];
+  // Every lane runs the same loops (bounds made uniform over the warp) and a term is added only
+  // where the index form adds it, so the lanes of a warp stay converged.  The terms and their
+  // order are those of the index form: for each fine cell i (x fastest in this thread's row of
+  // children), each of i's transfers to I, each stencil neighbour j, each of j's transfers.  Cell
+  // coordinates are carried along instead of decoded from indices: qi from the loop, qj from
+  // qi + offset, the coarse coordinates of j's transfers from the table (mgtq).
+  const bool rowok = row_local < rpb && I < cl.count && m.active<T>(l + 1, I);
+  const I3 qc = rowok ? m.coord(l + 1, I) : mk(0, 0, 0);
+  int lo[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
+  if (rowok)
     for (int a = 0; a < 3; a++) child_range(D, l, a, qc[a], lo[a], ext[a]);
-    int gz = g / ey, gy = g % ey;
-    // Cell coordinates are carried along instead of decoded from indices: qi from the loop, qj
-    // from qi + offset, and the coarse coordinates of j's transfers from the table (mgtq).  The
-    // terms and their order are those of the index form: for each fine cell i (x fastest in this
-    // thread's row of children), each of i's transfers to I, each stencil neighbour j, each of j's
-    // transfers.
-    const long long tstride = fl.count;
-    for (int gx = 0; gx < ext[0]; gx++) {
-      I3 qi = mk(lo[0] + gx, lo[1] + gy, lo[2] + gz);
-      if (!m.wrap_q(l, qi)) continue;
-      const int i = qi.x + fl.nx * (qi.y + fl.ny * qi.z);
-      if (!m.active<T>(l, i)) continue;
-      int li[8];
-      float lw[8];
-      int nl = m.transfers(l, i, li, lw);
-      for (int a = 0; a < nl; a++) {
-        if (li[a] != I) continue;
-        for (int k = 0; k < fl.stencil; k++) {
-          // every load of one neighbour (its activity, the coefficient, its transfers) is issued
-          // before the first test; a neighbour outside the grid loads from i instead
-          const I3 off = offs[k];
-          I3 qj = addI(qi, off);
-          const bool in = m.wrap_q(l, qj);
-          const int j = in ? qj.x + fl.nx * (qj.y + fl.ny * qj.z) : i;
-          if (!in) qj = qi;
-          bool uniq = true;
-          long long maddr = -1;
-          if (l > 0) {
-            // unique_neighbor and coefficient() of two active cells
-            uniq = eqI(m.delta_q(l, qi, qj), off);
-            const bool ilo = i <= j;
-            const I3 d = ilo ? m.delta_q(l, qi, qj) : m.delta_q(l, qj, qi);
-            if (!(abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2)) maddr = fl.moff + (long long)(ilo ? i : j) * 125 + MG::slot(d);
-          }
-          const bool actj = m.active<T>(l, j);
-          const float coef = l == 0 ? (k == 0 ? m.fine_coef(12, i) : -m.fine_coef(5 + k, i)) : (maddr >= 0 ? D.mgmat[maddr] : 0.f);
-          const long long tj = fl.toff + j;
-          float wv[8];
-          unsigned long long qv[8];
+  const int gz = g / ey, gy = g % ey;
+  const long long tstride = fl.count;
+  const int nxi = __reduce_max_sync(0xffffffffu, (unsigned)ext[0]);
+  for (int gx = 0; gx < nxi; gx++) {
+    I3 qi = mk(lo[0] + gx, lo[1] + gy, lo[2] + gz);
+    bool cell = rowok && gx < ext[0] && m.wrap_q(l, qi);
+    if (!cell) qi = mk(0, 0, 0);
+    const int i = qi.x + fl.nx * (qi.y + fl.ny * qi.z);
+    cell = cell && m.active<T>(l, i);
+    int li[8];
+    float lw[8];
+    const int nl = cell ? m.transfers(l, i, li, lw) : 0;
+    unsigned match = 0;
+    for (int a = 0; a < nl; a++)
+      if (li[a] == I) match |= 1u << a;
+    const int nmatch = __popc(match);
+    const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)nmatch);
+    for (int r = 0; r < rounds; r++) {
+      const bool has = r < nmatch;
+      const int a = has ? __ffs(match) - 1 : 0;
+      if (has) match &= match - 1;
+      const float lwa = has ? lw[a] : 0.f;
+      for (int k = 0; k < fl.stencil; k++) {
+        // every load of one neighbour (its activity, the coefficient, its transfers) is issued
+        // before the first test; a neighbour outside the grid loads from i instead
+        const I3 off = offs[k];
+        I3 qj = addI(qi, off);
+        const bool in = m.wrap_q(l, qj);
+        const int j = in ? qj.x + fl.nx * (qj.y + fl.ny * qj.z) : i;
+        if (!in) qj = qi;
+        bool uniq = true;
+        long long maddr = -1;
+        if (l > 0) {
+          // unique_neighbor and coefficient() of two active cells
+          uniq = eqI(m.delta_q(l, qi, qj), off);
+          const bool ilo = i <= j;
+          const I3 d = ilo ? m.delta_q(l, qi, qj) : m.delta_q(l, qj, qi);
+          if (!(abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2)) maddr = fl.moff + (long long)(ilo ? i : j) * 125 + MG::slot(d);
+        }
+        const bool actj = m.active<T>(l, j);
+        const float aij = l == 0 ? (k == 0 ? m.fine_coef(12, i) : -m.fine_coef(5 + k, i)) : (maddr >= 0 ? D.mgmat[maddr] : 0.f);
+        const long long tj = fl.toff + j;
+        float wv[8];
+        unsigned long long qv[8];
 #pragma unroll
-          for (int b = 0; b < 8; b++)
-            if (b < fl.twidth) {
-              wv[b] = D.mgtw[tj + b * tstride];
-              qv[b] = D.mgtq[tj + b * tstride];
-            }
-          if (!in || !actj) continue;
-          if (!uniq) continue;
-          const float aij = coef;
-          if (aij == 0.f) continue;
-          const float al = aij * lw[a];
-#pragma unroll
-          for (int b = 0; b < 8; b++) {
-            if (b >= fl.twidth || !(wv[b] > 0.f)) continue;
-            const I3 d = m.delta_q(l + 1, qc, MG::unpack(qv[b]));
-            if (abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2) {
-              D.c[7] = 31;
-              continue;
-            }
-            part[MG::slot(d) * GT + t] += al * wv[b];
+        for (int b = 0; b < 8; b++)
+          if (b < fl.twidth) {
+            wv[b] = D.mgtw[tj + b * tstride];
+            qv[b] = D.mgtq[tj + b * tstride];
           }
+        const bool use = has && in && actj && uniq && aij != 0.f;
+        const float al = aij * lwa;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          if (b >= fl.twidth) break;
+          const bool ub = use && wv[b] > 0.f;
+          const I3 d = m.delta_q(l + 1, qc, MG::unpack(qv[b]));
+          const bool far = abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2;
+          if (ub && far) D.c[7] = 31;
+          if (ub && !far) part[MG::slot(d) * GT + t] += al * wv[b];
         }
       }
     }
