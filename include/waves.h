@@ -233,6 +233,16 @@ waves_status waves_render(waves_handle* h, const waves_render_params* p, float* 
 /* The same into caller device buffers (16-byte aligned), enqueued on the handle's stream. */
 waves_status waves_render_device(waves_handle* h, const waves_render_params* p, void* rgba, void* trace);
 
+/* Telemetry history, each buffer sized by history_capacity (cap); any pointer may be NULL.
+ *   history[16 cap]: per trial four float4 rows (coupled_motion.glslinc:338-340): the three VOF
+ *     sweeps (min F, max F, summed change, summed |change|), then (accepted time, dt, state:
+ *     -failure code or 1 pending / 0 done, accepted steps) (op 44, pressure_pass.glslinc).
+ *   coastal[20 cap]: per accepted step five float4 rows of the coastal ledger and the eight gauges
+ *     (coastal_pass.glslinc:60-80, op 89).
+ *   audit[64 + 32 cap]: the multigrid hierarchy audit words, a 64-word header then one 32-word row
+ *     per rebuild (pressure_hierarchy_state.glsl:55-59,67). */
+waves_status waves_get_history(waves_handle* h, float* history, float* coastal, uint32_t* audit);
+
 /* Bank access.  bank = 0/1 physical bank, -1 the accepted bank.  A bank is
  * [F: N][u: (nx+1) ny nz][v: nx (ny+1) nz][w: nx ny (nz+1)][p: N] floats, x-fastest. */
 size_t waves_bank_floats(const waves_handle* h);

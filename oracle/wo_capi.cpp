@@ -140,6 +140,13 @@ void wo_mg_state(void* h, uint32_t* out32) {
     return 0;
   });
 }
+// The whole audit state: the 64-word header, then 32 words per rebuild.
+void wo_mg_audit(void* h, uint32_t* out, size_t words) {
+  with(h, [&](auto& s) {
+    for (size_t k = 0; k < words && k < s.mg.state.size(); k++) out[k] = s.mg.state[k];
+    return 0;
+  });
+}
 // Step history rows (4 per trial) and coastal history rows (5 per step), vec4 each.
 void wo_get_history(void* h, float* hist, float* chist) {
   with(h, [&](auto& s) {

@@ -53,6 +53,7 @@ def lib():
             "wo_mg_stencil": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
             "wo_mg_state": (None, [vp, C.POINTER(C.c_uint32)]),
             "wo_get_history": (None, [vp, fp, fp]),
+            "wo_mg_audit": (None, [vp, C.POINTER(C.c_uint32), C.c_size_t]),
             "wo_cube_volume": (C.c_float, [C.c_float] * 4),
             "wo_inverse_volume": (C.c_float, [C.c_float] * 4),
             "wo_cube_volume_d": (C.c_double, [C.c_double] * 4),
@@ -168,6 +169,12 @@ class Oracle:
         ch = np.empty(20 * self.cap, dtype=np.float32)
         self.L.wo_get_history(self.h, _fp(h), _fp(ch))
         return h.reshape(-1, 4), ch.reshape(-1, 4)
+
+    def audit(self):
+        words = 64 + 32 * max(self.cap, 1)
+        out = np.zeros(words, dtype=np.uint32)
+        self.L.wo_mg_audit(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)), words)
+        return out
 
     def levels(self):
         dims = (C.c_int * 36)()

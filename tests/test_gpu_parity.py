@@ -179,3 +179,36 @@ def test_surface_export_parity(gpu_lib):
     assert g.control()[2] == 3 and g.control()[7] == 4
     check_export(g, o)
     g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["beach_slope", "tank_small"])
+def test_history_parity(gpu_lib, name):
+    """Telemetry history read back through waves_get_history against the oracle: per-trial sweep and
+    trial rows, the coastal ledger and gauge rows, and the hierarchy audit words."""
+    cfg = CASES[name]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for s in (g, o):
+        s.request_steps(STEPS)
+        s.run()
+    trials, steps = int(g.control()[32]), int(g.control()[2])
+    assert trials == int(o.control()[32]) and steps == STEPS
+    hg, cg, ag = g.history()
+    ho, co = o.history()
+    ao = o.audit()
+    for t in range(trials):
+        sweeps_g, sweeps_o = hg[4 * t:4 * t + 3], ho[4 * t:4 * t + 3]
+        assert np.array_equal(sweeps_g[:, :2], sweeps_o[:, :2]), (t, sweeps_g, sweeps_o)  # min / max F
+        assert np.allclose(sweeps_g[:, 2:], sweeps_o[:, 2:], rtol=1e-6, atol=1e-12), (t, sweeps_g, sweeps_o)
+        assert np.array_equal(hg[4 * t + 3], ho[4 * t + 3]), (t, hg[4 * t + 3], ho[4 * t + 3])
+    if cfg.coastal:
+        rows_g, rows_o = cg[:5 * steps], co[:5 * steps]
+        assert np.abs(rows_o).sum() > 0
+        assert np.allclose(rows_g, rows_o, rtol=1e-6, atol=1e-9), np.argwhere(~np.isclose(rows_g, rows_o, rtol=1e-6, atol=1e-9))[:5]
+    builds = int(ag[13])
+    assert builds >= 1 and builds == int(ao[13])
+    words = 64 + 32 * builds
+    m = first_mismatch(ag[:words].astype(np.int64), ao[:words].astype(np.int64))
+    assert not m, f"audit: {m}"
+    g.close()

@@ -221,6 +221,17 @@ class WavesSolver:
         self._ck(self.lib.waves_export_surface_device(self.h, C.c_void_p(planes_ptr), C.c_void_p(kinds_ptr),
                                                       C.c_void_p(clock_ptr) if clock_ptr else None))
 
+    def history(self):
+        """waves_get_history: (per-trial rows (4 cap, 4), coastal rows (5 cap, 4), audit words)."""
+        cap = max(self.cfg.history_capacity, 1)
+        hist = np.empty(16 * cap, dtype=np.float32)
+        coast = np.empty(20 * cap, dtype=np.float32)
+        audit = np.empty(64 + 32 * cap, dtype=np.uint32)
+        self._ck(self.lib.waves_get_history(self.h, hist.ctypes.data_as(C.POINTER(C.c_float)),
+                                            coast.ctypes.data_as(C.POINTER(C.c_float)),
+                                            audit.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return hist.reshape(-1, 4), coast.reshape(-1, 4), audit
+
     def render_params(self, width=1280, height=720, **overrides):
         """waves_render_params_default for this configuration, with field overrides."""
         from .abi import WavesRenderParams

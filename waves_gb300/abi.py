@@ -214,6 +214,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_set_control",
     "waves_export_surface",
     "waves_export_surface_device",
+    "waves_get_history",
     "waves_render_params_default",
     "waves_render",
     "waves_render_device",
@@ -258,6 +259,7 @@ def declare(lib):
         "waves_export_surface": (C.c_int, [h, P(C.c_float), P(C.c_float)]),
         "waves_export_surface_device": (C.c_int, [h, C.c_void_p, C.c_void_p, C.c_void_p]),
         "waves_render_params_default": (None, [P(WavesRenderParams), cfgp, C.c_int32, C.c_int32]),
+        "waves_get_history": (C.c_int, [h, P(C.c_float), P(C.c_float), P(C.c_uint32)]),
         "waves_render": (C.c_int, [h, P(WavesRenderParams), P(C.c_float), P(C.c_float)]),
         "waves_render_device": (C.c_int, [h, P(WavesRenderParams), C.c_void_p, C.c_void_p]),
         "waves_bank_floats": (C.c_size_t, [h]),

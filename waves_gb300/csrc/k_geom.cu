@@ -550,35 +550,59 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
 }
 
 // ---------------------------------------------------------------- ops 44, 85, 89 (one block)
-__global__ void __launch_bounds__(NT) k_trial_end(const __grid_constant__ Dev D) {
+// One block of kTrialEndThreads threads.  Op 85 (gauges of the accepted state): for each of the
+// eight gauge columns x, the column heights oy + sum_y (solid ? 1 : F) hy of every z, each summed
+// in y order, then the gauge's mean over z in z order.  The terms of kGaugeZ planes at a time are
+// loaded by the whole block into shared memory (every load independent), then summed in that order.
+constexpr int kTrialEndThreads = 1024, kGaugeVals = 10240, kGaugeMaxZ = 128;
+__global__ void __launch_bounds__(kTrialEndThreads) k_trial_end(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
-  __shared__ float cols[8 * 128];
+  __shared__ float vals[kGaugeVals];
+  __shared__ float cols[8 * kGaugeMaxZ];
+  __shared__ int gx[8];
   Grid g(D);
   const float* A = bank_ptr(D, acc_bank(D));
   double* c = D.c;
   if (D.coastal) {
-    // op 85: gauges of the accepted state; the column heights of 128 z planes at a time, each
-    // gauge's sum taken in z order
+    if (threadIdx.x < 8) {
+      float begin = D.forcing[0] + D.forcing[1] + .4f;
+      float end = D.ox + (float)D.nx * D.hx - (D.shape == 6 ? D.forcing[1] + .4f : 1.0f);
+      float tt = (float)threadIdx.x / 7.f;
+      float pos = begin * (1.f - tt) + end * tt;
+      gx[threadIdx.x] = min(max((int)((pos - D.ox) / D.hx), 0), D.nx - 1);
+    }
+    __syncthreads();
+    const int ny = D.ny;
+    const int zc = min(kGaugeMaxZ, max(1, kGaugeVals / (8 * ny)));
+    const bool staged = 8 * ny <= kGaugeVals;
     float height = 0.f;
-    for (int z0 = 0; z0 < D.nz; z0 += 128) {
-      for (int t = threadIdx.x; t < 8 * 128; t += NT) {
-        const int gi = t / 128, z = z0 + t % 128;
-        if (z >= D.nz) continue;
-        float begin = D.forcing[0] + D.forcing[1] + .4f;
-        float end = D.ox + (float)D.nx * D.hx - (D.shape == 6 ? D.forcing[1] + .4f : 1.0f);
-        float tt = (float)gi / 7.f;
-        float pos = begin * (1.f - tt) + end * tt;
-        int x = min(max((int)((pos - D.ox) / D.hx), 0), D.nx - 1);
+    for (int z0 = 0; z0 < D.nz; z0 += zc) {
+      const int nzc = min(zc, D.nz - z0);
+      if (staged) {
+        for (int t = threadIdx.x; t < 8 * nzc * ny; t += kTrialEndThreads) {
+          const int gi = t / (nzc * ny), r = t - gi * (nzc * ny), zl = r / ny, y = r - zl * ny;
+          const I3 q = mk(gx[gi], y, z0 + zl);
+          vals[t] = (g.solid(q) ? 1.f : A[g.index3(q)]) * D.hy;
+        }
+        __syncthreads();
+        if (threadIdx.x < 8 * nzc) {
+          const float* v = vals + threadIdx.x * ny;  // gauge threadIdx.x / nzc, plane threadIdx.x % nzc
+          float column = D.oy;
+          for (int y = 0; y < ny; y++) column += v[y];
+          cols[threadIdx.x] = column;
+        }
+      } else if (threadIdx.x < 8 * nzc) {
+        const int gi = threadIdx.x / nzc, z = z0 + threadIdx.x % nzc;
         float column = D.oy;
-        for (int y = 0; y < D.ny; y++) {
-          I3 q = mk(x, y, z);
+        for (int y = 0; y < ny; y++) {
+          const I3 q = mk(gx[gi], y, z);
           column += (g.solid(q) ? 1.f : A[g.index3(q)]) * D.hy;
         }
-        cols[t] = column;
+        cols[threadIdx.x] = column;
       }
       __syncthreads();
       if (threadIdx.x < 8)
-        for (int z = z0; z < D.nz && z < z0 + 128; z++) height += cols[threadIdx.x * 128 + (z - z0)];
+        for (int zl = 0; zl < nzc; zl++) height += cols[threadIdx.x * nzc + zl];
       __syncthreads();
     }
     if (threadIdx.x < 8) c[80 + threadIdx.x] = (double)(height / (float)D.nz);
@@ -749,7 +773,7 @@ void launch_post(const Dev& D, cudaStream_t s) {
   pdl_launch(k_accept, grid_for(D.N), NT, 0, s, D);
 }
 void launch_ext_masks(const Dev& D, cudaStream_t s) { pdl_launch(k_ext_masks, grid_for(D.NF), NT, 0, s, D); }
-void launch_trial_end(const Dev& D, cudaStream_t s) { pdl_launch(k_trial_end, 1, NT, 0, s, D); }
+void launch_trial_end(const Dev& D, cudaStream_t s) { pdl_launch(k_trial_end, 1, kTrialEndThreads, 0, s, D); }
 void launch_export(const Dev& D, cudaStream_t s, float4* planes, float* kinds, float4* clock) {
   pdl_launch(k_export, grid_for(D.N), NT, 0, s, D, planes, kinds, clock);
 }

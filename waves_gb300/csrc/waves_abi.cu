@@ -1303,6 +1303,17 @@ waves_status waves_render(waves_handle* h, const waves_render_params* p, float* 
   return WAVES_OK;
 }
 
+waves_status waves_get_history(waves_handle* h, float* history, float* coastal, uint32_t* audit) {
+  if (!h) return WAVES_INVALID_ARG;
+  cudaSetDevice(h->cfg.device);
+  const size_t cap = (size_t)std::max(h->cfg.history_capacity, 1);
+  if (history) CK(cudaMemcpyAsync(history, h->D.history, 16 * cap * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  if (coastal) CK(cudaMemcpyAsync(coastal, h->D.chistory, 20 * cap * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  if (audit) CK(cudaMemcpyAsync(audit, h->D.hstate, (64 + 32 * cap) * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return WAVES_OK;
+}
+
 size_t waves_bank_floats(const waves_handle* h) { return h ? (size_t)h->D.S : 0; }
 
 waves_status waves_get_bank(waves_handle* h, int32_t bank, float* out) {
