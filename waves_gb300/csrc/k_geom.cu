@@ -384,6 +384,12 @@ __global__ void __launch_bounds__(NT) k_ext_step(const __grid_constant__ Dev D, 
     if (source >= 0) {
       F3 dl = g.periodic_delta(q, unpack_coords(source));
       best = dot3(dl, dl);
+      // a face that is its own source keeps it: no neighbour's source is nearer, and one at the
+      // same distance is this face, not a smaller index
+      if (best == 0.f) {
+        out[f] = source;
+        return;
+      }
     }
     for (int a = 0; a < 3; a++)
       for (int sign = -1; sign <= 1; sign += 2) {
