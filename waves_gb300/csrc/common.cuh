@@ -485,6 +485,98 @@ DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (
 }
 
 
+// Block maxima of K FP32 values: shuffle trees per warp, one barrier, the warps combined by
+// threads 0..K-1.  Maxima are independent of the order of combination.
+template <int NT, int K> DI void block_max_f(const float (&vals)[K], float (*shw)[NT / 32], float* tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    float m = vals[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float x = __shfl_down_sync(0xffffffffu, m, o);
+      m = m < x ? x : m;
+    }
+    if (lane == 0) shw[k][warp] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float m = shw[threadIdx.x][0];
+    for (int w = 1; w < NT / 32; w++) m = m < shw[threadIdx.x][w] ? shw[threadIdx.x][w] : m;
+    tot[threadIdx.x] = m;
+  }
+  __syncthreads();
+}
+
+// last_block_reduce with KD FP64 components (sums or maxima, `ops`) and KF FP32 maxima (the
+// maxima of FP32 values need no FP64 instructions: the same value results in either precision).
+// The FP32 partials follow the FP64 ones in D.part (KD + KF <= 9).
+template <int NT, int KD, int KF>
+DI bool last_block_reduce_mf(const Dev& D, int site, const double* vals, const int* ops, const float (&fvals)[KF],
+                             double* out, float (&fout)[KF]) {
+  static_assert(KD + KF <= 9, "partials buffer holds 9 values per block");
+  __shared__ double sh[(KD > 0 ? KD : 1) * NT];
+  __shared__ double tot[KD > 0 ? KD : 1];
+  __shared__ float shw[KF][NT / 32];
+  __shared__ float totf[KF];
+  __shared__ bool am_last;
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  double* part = D.part;
+  float* partf = (float*)(D.part + (size_t)KD * nb);
+  int opk[KD > 0 ? KD : 1];
+  if constexpr (KD > 0) {
+    double v[KD];
+#pragma unroll
+    for (int k = 0; k < KD; k++) {
+      v[k] = vals[k];
+      opk[k] = ops[k];
+    }
+    block_reduce_k<NT, KD>(v, opk, sh, tot);
+  }
+  block_max_f<NT, KF>(fvals, shw, totf);
+  if constexpr (KD > 0)
+    if (threadIdx.x < KD) part[(size_t)threadIdx.x * nb + bid] = tot[threadIdx.x];
+  if (threadIdx.x < KF) partf[(size_t)threadIdx.x * nb + bid] = totf[threadIdx.x];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int prev = atomicAdd(&D.count[site], 1u);
+    am_last = (prev == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  if constexpr (KD > 0) {
+    double acc[KD];
+#pragma unroll
+    for (int k = 0; k < KD; k++) {
+      acc[k] = opk[k] == 0 ? 0.0 : -1e300;
+      for (int b = threadIdx.x; b < nb; b += NT) {
+        double p = __ldcg(&part[(size_t)k * nb + b]);
+        acc[k] = opk[k] == 0 ? acc[k] + p : (acc[k] < p ? p : acc[k]);
+      }
+    }
+    block_reduce_k<NT, KD>(acc, opk, sh, tot);
+#pragma unroll
+    for (int k = 0; k < KD; k++) out[k] = tot[k];
+  }
+  float accf[KF];
+#pragma unroll
+  for (int k = 0; k < KF; k++) {
+    accf[k] = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += NT) {
+      const float p = __ldcg(&partf[(size_t)k * nb + b]);
+      accf[k] = accf[k] < p ? p : accf[k];
+    }
+  }
+  block_max_f<NT, KF>(accf, shw, totf);
+#pragma unroll
+  for (int k = 0; k < KF; k++) fout[k] = totf[k];
+  if (threadIdx.x == 0) D.count[site] = 0;
+  return true;
+}
+
 // ---------------------------------------------------------------- PCG control (pressure_core.glslinc:156-179)
 DI bool solving(const Dev& D) { return D.c[4] > 0.5 && D.c[6] < 0.5 && D.c[7] < 0.5; }
 DI bool pressure_setup(const Dev& D) { return D.c[5] > .5 || D.c[57] == 2; }

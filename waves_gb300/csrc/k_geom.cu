@@ -230,22 +230,21 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
   if (!on && !bounds) return;
   Geo G(D, op);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  double v[2] = {-1e300, -1e300};
+  float v[2] = {-INFINITY, -INFINITY};
   if (i < D.N) {
     if (on) D.plane[i] = G.reconstruct(G.g.coord(i));
     if (bounds) {
       float f = G.Cb[i];
       float a = f, b = f;
       if (isnan(f) || isinf(f)) { a = -1e30f; b = 1e30f; }
-      v[0] = -(double)a;
-      v[1] = (double)b;
+      v[0] = -a;
+      v[1] = b;
     }
   }
   if (!bounds) return;
-  const int ops[2] = {1, 1};
-  double out[2];
-  if (last_block_reduce<NT, 2>(D, kSiteBounds, v, ops, out) && threadIdx.x == 0) {
-    float minimum = mnf(1.f, (float)(-out[0])), maximum = mxf(0.f, (float)out[1]);
+  float out[2];
+  if (last_block_reduce_mf<NT, 0, 2>(D, kSiteBounds, nullptr, nullptr, v, nullptr, out) && threadIdx.x == 0) {
+    float minimum = mnf(1.f, -out[0]), maximum = mxf(0.f, out[1]);
     D.c[88] = minimum;
     D.c[89] = maximum;
     if (minimum < 0.f || maximum > 1.f) { D.c[7] = 23; D.c[3] += 1; }
@@ -472,8 +471,9 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
   Geo G(D, 12);
   const Grid& g = G.g;
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  // 0 max courant, 1 sum res^2, 2 max dt|div|, 3 max speed, 4 max hydro error, 5 volume
-  double v[6] = {0, 0, 0, 0, 0, 0};
+  // FP64 sums: 0 res^2, 1 volume; FP32 maxima: 0 courant dt, 1 dt|div|, 2 speed, 3 hydro error
+  double v[2] = {0, 0};
+  float fv[4] = {0.f, 0.f, 0.f, 0.f};
   if (i < D.N) {
     I3 q = g.coord(i);
     const long long P = D.N + D.NF;
@@ -489,11 +489,11 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
     }
     float cr = D.max_face_cfl ? mxf(s[0] / D.hx, mxf(s[1] / D.hy, s[2] / D.hz))
                               : (s[0] / D.hx) * 1.f + (s[1] / D.hy) * 1.f + (s[2] / D.hz) * 1.f;
-    v[0] = (double)(cr * G.dt);
+    fv[0] = cr * G.dt;
     bool w = D.kind[i] > 0;
     float dv = w ? G.divergence(q) : 0.f;
     float rr = w ? 1000.f / G.dt * dv : 0.f;
-    v[1] = (double)rr * (double)rr;
+    v[0] = (double)rr * (double)rr;
     float div = w ? G.dt * fabsf(dv) : 0.f;
     float err = w ? fabsf(p - 9810.0f * (g.eta(q) - g.center(q).y)) : 0.f;
     float f = G.Cb[i];
@@ -502,20 +502,21 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
       div = speed = err = 1e30f;
       vol = 1e30;
     }
-    v[2] = div;
-    v[3] = speed;
-    v[4] = err;
-    v[5] = vol;
+    fv[1] = div;
+    fv[2] = speed;
+    fv[3] = err;
+    v[1] = vol;
   }
-  const int ops[6] = {1, 0, 1, 1, 1, 0};
-  double out[6];
-  if (last_block_reduce<NT, 6>(D, kSiteAccept, v, ops, out) && threadIdx.x == 0) {
+  const int ops[2] = {0, 0};
+  double out[2];
+  float fout[4];
+  if (last_block_reduce_mf<NT, 2, 4>(D, kSiteAccept, v, ops, fv, out, fout) && threadIdx.x == 0) {
     double* c = D.c;
     double dtd = (double)G.dt;
     // op 36
-    c[27] = out[0];
+    c[27] = (double)fout[0];
     // op 66
-    double r2 = out[1];
+    double r2 = out[0];
     auto scaled = [&](double sq) { return dtd * dtd / 1000 * sqrt(sq > 0 ? sq : 0.0); };
     double tol = (double)D.tol;
     auto conv = [&](double res2, double rhs2) {
@@ -526,8 +527,8 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
     c[63] = scaled(r2);
     c[61] = conv(r2, c[59]) ? 1 : 0;
     // op 13
-    float vx = (float)out[2], vy = (float)out[3], vz = (float)out[4];
-    double vw = out[5];
+    float vx = fout[1], vy = fout[2], vz = fout[3];
+    double vw = out[1];
     c[14] = vx; c[15] = vy; c[16] = vz; c[17] = vw;
     if ((vx >= 1e-4f || c[61] < .5) && vy < 1e20f && c[19] < .5 && c[58] < 4) {
       c[57] = 1; c[58] += 1; c[6] = 0;

@@ -234,8 +234,10 @@ __global__ void __launch_bounds__(NT, 6) k_sweep_update(const __grid_constant__ 
   int sa = ((int)D.c[2] + (int)D.c[21]) % 3;
   int sweep = (int)D.c[21];
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  // reductions: -min f, max f, sum change, sum |change|, rounding ledger, compression, top, in, out
-  double v[9] = {-1e20, -1e20, 0, 0, 0, 0, 0, 0, 0};
+  // FP32 maxima: -min f, max f; FP64 sums: change, |change|, rounding ledger, compression, top,
+  // in, out
+  float fv[2] = {-1e20f, -1e20f};
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};
   if (i < D.N) {
     I3 q = m.g.coord(i), r = ax(q, sa, 1);
     float cq, cr;
@@ -252,32 +254,33 @@ __global__ void __launch_bounds__(NT, 6) k_sweep_update(const __grid_constant__ 
     else m.Cb[i] = out;
     float a = f, b = f;
     if (isnan(f) || isinf(f)) { a = -1e30f; b = 1e30f; }
-    v[0] = -(double)a;
-    v[1] = (double)b;
-    v[2] = (double)change;
-    v[3] = (double)fabsf(change);
-    v[4] = ((double)out - (double)fin - (double)net - (double)correction) * D.cell_d;
-    v[5] = (double)correction * D.cell_d;
-    if (sa == 1 && q.y == D.ny - 1) v[6] = (double)fr_ * D.cell_d;
+    fv[0] = -a;
+    fv[1] = b;
+    v[0] = (double)change;
+    v[1] = (double)fabsf(change);
+    v[2] = ((double)out - (double)fin - (double)net - (double)correction) * D.cell_d;
+    v[3] = (double)correction * D.cell_d;
+    if (sa == 1 && q.y == D.ny - 1) v[4] = (double)fr_ * D.cell_d;
     if (D.coastal && sa == 0 && q.x == 0) {
       double fl = (double)fq * D.cell_d;
-      v[7] = fl > 0 ? fl : 0.0;
-      v[8] = -fl > 0 ? -fl : 0.0;
+      v[5] = fl > 0 ? fl : 0.0;
+      v[6] = -fl > 0 ? -fl : 0.0;
     }
   }
-  const int ops[9] = {1, 1, 0, 0, 0, 0, 0, 0, 0};
-  double out[9];
-  if (last_block_reduce<NT, 9>(D, kSiteSweep, v, ops, out) && threadIdx.x == 0) {
+  const int ops[7] = {0, 0, 0, 0, 0, 0, 0};
+  double out[7];
+  float fout[2];
+  if (last_block_reduce_mf<NT, 7, 2>(D, kSiteSweep, v, ops, fv, out, fout) && threadIdx.x == 0) {
     double* c = D.c;
-    float vmin = (float)(-out[0]), vmax = (float)out[1];
+    float vmin = -fout[0], vmax = fout[1];
     long long step = (long long)c[32] - 1;
-    if (c[32] >= 1 && step < D.hist_cap) D.history[step * 4 + sweep] = make_float4(vmin, vmax, (float)out[2], (float)out[3]);
-    c[22] += out[2] * D.cell_d;
-    c[23] += out[3] * D.cell_d;
-    c[kSweepRound] += out[4];
-    c[kSweepComp] += out[5];
-    c[39] += out[6];
-    if (D.coastal) { c[65] += out[7]; c[66] += out[8]; }
+    if (c[32] >= 1 && step < D.hist_cap) D.history[step * 4 + sweep] = make_float4(vmin, vmax, (float)out[0], (float)out[1]);
+    c[22] += out[0] * D.cell_d;
+    c[23] += out[1] * D.cell_d;
+    c[kSweepRound] += out[2];
+    c[kSweepComp] += out[3];
+    c[39] += out[4];
+    if (D.coastal) { c[65] += out[5]; c[66] += out[6]; }
     if (vmin < -1e-6f || vmax > 1.f + 1e-6f) { c[7] = 10 + c[21]; c[3] += 1; }
     c[21] += 1;
   }
