@@ -824,7 +824,8 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
   grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
   const Cell0 c = cell0(D);
-  double v[4] = {0, 0, 0, 0};
+  double v[3] = {0, 0, 0};
+  float vmax[1] = {0.f};
   if (c.ok) {
     const T* __restrict__ x = field0<T>(D, source);
     T* v7 = field0<T>(D, 7);
@@ -845,13 +846,15 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
       v[0] = (double)rr * (double)z;
       v[1] = (double)rr * (double)rr;
       v[2] = (double)bb * (double)bb;
-      v[3] = (double)fabsf(rr);
+      vmax[0] = fabsf(rr);
     }
   }
   if (fin < 0) return;
-  const int ops[4] = {0, 0, 0, 1};
+  const int ops[3] = {0, 0, 0};
   double out[4];
-  if (last_block_reduce<NT, 4>(D, kSiteRZ, v, ops, out) && threadIdx.x == 0) {
+  float fout[1];
+  if (last_block_reduce_mf<NT, 3, 1>(D, kSiteRZ, v, ops, vmax, out, fout) && threadIdx.x == 0) {
+    out[3] = (double)fout[0];
     if (phase == 0) finalize_op4(D, out);
     else finalize_op9(D, out);
   }
@@ -1162,7 +1165,8 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __gri
   if (!phase_on(D, phase)) return;
   MG m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  double v[4] = {0, 0, 0, 0};
+  double v[3] = {0, 0, 0};
+  float vmax[1] = {0.f};
   if (i < D.N) {
     float r = D.r[i], z = ld_val(m.field<T>(f, 0)[i]), b = D.b[i];
     D.z[i] = z;
@@ -1170,11 +1174,13 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __gri
     v[0] = (double)r * (double)z;
     v[1] = (double)r * (double)r;
     v[2] = (double)b * (double)b;
-    v[3] = (double)fabsf(r);
+    vmax[0] = fabsf(r);
   }
-  const int ops[4] = {0, 0, 0, 1};
+  const int ops[3] = {0, 0, 0};
   double out[4];
-  if (last_block_reduce<NT, 4>(D, kSiteRZ, v, ops, out) && threadIdx.x == 0) {
+  float fout[1];
+  if (last_block_reduce_mf<NT, 3, 1>(D, kSiteRZ, v, ops, vmax, out, fout) && threadIdx.x == 0) {
+    out[3] = (double)fout[0];
     if (phase == 0) finalize_op4(D, out);
     else finalize_op9(D, out);
   }

@@ -112,13 +112,12 @@ __global__ void __launch_bounds__(NT) k_cfl(const __grid_constant__ Dev D) {
   if (!setup_on(D)) return;
   Motion m(D);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  double v[1] = {0.0};
-  if (i < D.N) v[0] = (double)m.courant_at(m.g.coord(i), m.A, true);
-  const int ops[1] = {1};
-  double out[1];
-  if (last_block_reduce<NT, 1>(D, kSiteCFL, v, ops, out) && threadIdx.x == 0) {
+  float v[1] = {0.f};
+  if (i < D.N) v[0] = m.courant_at(m.g.coord(i), m.A, true);
+  float out[1];
+  if (last_block_reduce_mf<NT, 0, 1>(D, kSiteCFL, nullptr, nullptr, v, nullptr, out) && threadIdx.x == 0) {
     double* c = D.c;
-    float rate = mxf(0.f, (float)out[0]);
+    float rate = mxf(0.f, out[0]);
     float d = mnf(D.dtcfg, D.cfl / mxf(rate, 1e-20f));
     if (c[29] > 0) d = mnf(d, (float)c[30]);
     c[20] = (double)d;

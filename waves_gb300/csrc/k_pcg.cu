@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
   const float* p = Cb + D.N + D.NF;
   float dt = (float)D.c[20];
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  double v[4] = {0, 0, 0, 0};
+  double v[3] = {0, 0, 0};
+  float vmax[1] = {0.f};
   if (i < D.N) {
     I3 q = g.coord(i);
     float r = 0.f, z = 0.f, bv = 0.f, diag = 1.f;
@@ -120,11 +121,13 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
     v[0] = (double)r * (double)z;
     v[1] = (double)r * (double)r;
     v[2] = (double)bv * (double)bv;
-    v[3] = (double)fabsf(r);
+    vmax[0] = fabsf(r);
   }
-  const int ops[4] = {0, 0, 0, 1};
+  const int ops[3] = {0, 0, 0};
   double out[4];
-  if (last_block_reduce<NT, 4>(D, kSiteCGInit, v, ops, out) && threadIdx.x == 0) {
+  float fout[1];
+  if (last_block_reduce_mf<NT, 3, 1>(D, kSiteCGInit, v, ops, vmax, out, fout) && threadIdx.x == 0) {
+    out[3] = (double)fout[0];
     // The V-cycle (and its own op 4) runs exactly when no failure is latched.
     if (D.c[7] > .5) finalize_op4(D, out);
   }
