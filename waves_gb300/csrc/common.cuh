@@ -422,13 +422,28 @@ struct MaxF { DI float operator()(float a, float b) const { return (a < b) ? b :
 // stores its values (one barrier), then warp w reduces value k = w, w + NT/32, ...: lane j
 // combines entries j, j + 32, j + 64, ... in that order, then a shuffle tree over the lanes.
 // The order is fixed, so the result is deterministic.  Totals land in tot[] (all threads).
+// A value whose entries are all +0.0 in the block totals +0.0 (sum or maximum) without FP64
+// instructions: each warp records which values it holds other bits of.
 template <int NT, int K>
 DI void block_reduce_k(const double (&vals)[K], const int (&ops)[K], double* sh, double* tot) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ unsigned nonzero[NT / 32];
+  unsigned mine = 0;
 #pragma unroll
-  for (int k = 0; k < K; k++) sh[k * NT + threadIdx.x] = vals[k];
+  for (int k = 0; k < K; k++) {
+    sh[k * NT + threadIdx.x] = vals[k];
+    if (__any_sync(0xffffffffu, __double_as_longlong(vals[k]) != 0)) mine |= 1u << k;
+  }
+  if (lane == 0) nonzero[warp] = mine;
   __syncthreads();
+  unsigned any = 0;
+#pragma unroll
+  for (int w = 0; w < NT / 32; w++) any |= nonzero[w];
   for (int k = warp; k < K; k += NT / 32) {
+    if (!((any >> k) & 1u)) {
+      if (lane == 0) tot[k] = 0.0;
+      continue;
+    }
     const bool mx = ops[k] != 0;
     double acc = sh[k * NT + lane];
 #pragma unroll

@@ -255,10 +255,14 @@ __global__ void __launch_bounds__(NT, 6) k_sweep_update(const __grid_constant__ 
     if (isnan(f) || isinf(f)) { a = -1e30f; b = 1e30f; }
     fv[0] = -a;
     fv[1] = b;
-    v[0] = (double)change;
-    v[1] = (double)fabsf(change);
-    v[2] = ((double)out - (double)fin - (double)net - (double)correction) * D.cell_d;
-    v[3] = (double)correction * D.cell_d;
+    // the FP64 ledger terms only where they can be other than zero
+    if (change != 0.f) {
+      v[0] = (double)change;
+      v[1] = (double)fabsf(change);
+    }
+    if (out != fin || net != 0.f || correction != 0.f)
+      v[2] = ((double)out - (double)fin - (double)net - (double)correction) * D.cell_d;
+    if (correction != 0.f) v[3] = (double)correction * D.cell_d;
     if (sa == 1 && q.y == D.ny - 1) v[4] = (double)fr_ * D.cell_d;
     if (D.coastal && sa == 0 && q.x == 0) {
       double fl = (double)fq * D.cell_d;
