@@ -493,11 +493,11 @@ __global__ void __launch_bounds__(NT) k_accept(const __grid_constant__ Dev D) {
     bool w = D.kind[i] > 0;
     float dv = w ? G.divergence(q) : 0.f;
     float rr = w ? 1000.f / G.dt * dv : 0.f;
-    v[0] = (double)rr * (double)rr;
+    if (rr != 0.f) v[0] = (double)rr * (double)rr;
     float div = w ? G.dt * fabsf(dv) : 0.f;
     float err = w ? fabsf(p - 9810.0f * (g.eta(q) - g.center(q).y)) : 0.f;
     float f = G.Cb[i];
-    double vol = (double)f * D.cell_d;
+    double vol = f != 0.f ? (double)f * D.cell_d : 0.0;
     if (isnan(div) || isnan(speed) || isnan(err) || isnan(f) || isinf(div) || isinf(speed) || isinf(err) || isinf(f)) {
       div = speed = err = 1e30f;
       vol = 1e30;

@@ -843,9 +843,12 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
       const float rr = D.r[c.i], z = ld_val(xs), bb = D.b[c.i];
       D.z[c.i] = z;
       if (phase == 0) D.d[c.i] = z;
-      v[0] = (double)rr * (double)z;
-      v[1] = (double)rr * (double)rr;
-      v[2] = (double)bb * (double)bb;
+      // FP64 terms only where they can be other than zero
+      if (rr != 0.f || !isfinite(z)) {
+        v[0] = (double)rr * (double)z;
+        v[1] = (double)rr * (double)rr;
+      }
+      if (bb != 0.f) v[2] = (double)bb * (double)bb;
       vmax[0] = fabsf(rr);
     }
   }
@@ -1171,9 +1174,11 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __gri
     float r = D.r[i], z = ld_val(m.field<T>(f, 0)[i]), b = D.b[i];
     D.z[i] = z;
     if (phase == 0) D.d[i] = z;
-    v[0] = (double)r * (double)z;
-    v[1] = (double)r * (double)r;
-    v[2] = (double)b * (double)b;
+    if (r != 0.f || !isfinite(z)) {
+      v[0] = (double)r * (double)z;
+      v[1] = (double)r * (double)r;
+    }
+    if (b != 0.f) v[2] = (double)b * (double)b;
     vmax[0] = fabsf(r);
   }
   const int ops[3] = {0, 0, 0};

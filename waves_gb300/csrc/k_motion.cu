@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(NT) k_compress(const __grid_constant__ Dev D) 
     }
     if (f > .5f) v[0] = (double)(m.dt * dv) * D.cell_d;
     if (f > .5f && pmA[i] < .5f) v[1] = 1.0;
-    v[2] = (double)f * D.cell_d;
+    if (f != 0.f) v[2] = (double)f * D.cell_d;
     if (f > .5f) v[3] = (double)(m.dt * raw) * D.cell_d;
     D.mci[i] = f > .5f ? 1.f : 0.f;
   }

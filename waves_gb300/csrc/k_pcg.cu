@@ -118,9 +118,12 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
     D.d[i] = z;
     D.diag[i] = diag;
     D.b[i] = bv;
-    v[0] = (double)r * (double)z;
-    v[1] = (double)r * (double)r;
-    v[2] = (double)bv * (double)bv;
+    // FP64 terms only where they can be other than zero
+    if (r != 0.f || !isfinite(z)) {
+      v[0] = (double)r * (double)z;
+      v[1] = (double)r * (double)r;
+    }
+    if (bv != 0.f) v[2] = (double)bv * (double)bv;
     vmax[0] = fabsf(r);
   }
   const int ops[3] = {0, 0, 0};
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D)
   if (i < D.N) {
     float qv = D.kind[i] > 0 ? operator_at(D, g, g.coord(i), i, D.d) : 0.f;
     D.q[i] = qv;
-    v[0] = (double)D.d[i] * (double)qv;
+    if (qv != 0.f) v[0] = (double)D.d[i] * (double)qv;  // dry cells add nothing
   }
   const int ops[1] = {0};
   double out[1];
