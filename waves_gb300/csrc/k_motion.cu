@@ -33,7 +33,6 @@ struct Motion {
     if (!g.face_in_bounds(q, axis) || g.wall_face(q, axis)) return 0.f;
     return A[g.face_index(q, axis)];
   }
-  DI float face_courant(I3 q, int axis) const { return old_face(q, axis) * dt / g.h(axis); }
   // transport_f (coupled_motion.glslinc:36-44)
   DI float transport_f(I3 q) const {
     q = g.wrap_cell(q);
@@ -455,35 +454,6 @@ struct Mac {
     float l0, l1v;
     for (int axis = 0; axis < 3; axis++) v[axis] = sample(x, axis, false, valid, l0, l1v);
     return v;
-  }
-  DI F3 velocity_checked(F3 x, bool& supported) const {
-    F3 v;
-    supported = true;
-    for (int axis = 0; axis < 3; axis++) {
-      bool valid;
-      float l0, l1v;
-      v[axis] = sample(x, axis, false, valid, l0, l1v);
-      supported = supported && valid;
-    }
-    return v;
-  }
-  DI float endpoint(F3 x, int component, bool forward, bool& supported, float& lim0, float& lim1) const {
-    float value = 0.f;
-    supported = true;
-    lim0 = 0.f;
-    lim1 = 0.f;
-    for (int axis = 0; axis < 3; axis++) {
-      bool valid;
-      float d0, d1;
-      float dv = sample(x, axis, axis == component && forward, valid, d0, d1);
-      supported = supported && valid;
-      if (axis == component) {
-        value = dv;
-        lim0 = d0;
-        lim1 = d1;
-      }
-    }
-    return value;
   }
   DI bool solid_at(F3 p) const {
     const Dev& D = m.D;
