@@ -29,7 +29,7 @@ def test_python_symbol_list_matches_header():
 
 
 def test_presets_without_gpu():
-    lib = waves_gebuild = waves_gb300.load(build_if_missing=True)
+    lib = waves_gb300.load(build_if_missing=True)
     beach = waves_gb300.config("beach")
     assert tuple(beach.n) == (310, 48, 80)
     assert abs(beach.wave[1] - 2.52502) < 1e-4  # lab_runner.gd:19-25 dispersion, T = 1.4 s, h = 0.45 m
@@ -60,3 +60,21 @@ def test_harness_argument_and_device_errors():
     if not torch.cuda.is_available():
         r = subprocess.run([HARNESS, "--preset", "tank", "--steps", "1"], capture_output=True, text=True)
         assert r.returncode == 2 and "waves_create" in r.stderr
+
+
+def test_render_defaults_without_gpu():
+    """waves_render_params_default: water.gdshader's look and presentation.gd's camera_preset(1),
+    the wide view when the domain is deeper than 1 m in z."""
+    import ctypes as C
+    from waves_gb300.abi import WavesRenderParams
+    lib = waves_gb300.load(build_if_missing=True)
+    p = WavesRenderParams()
+    beach = waves_gb300.config("beach")
+    lib.waves_render_params_default(C.byref(p), C.byref(beach), 640, 360)
+    assert (p.width, p.height, p.mode, p.orthographic) == (640, 360, 1, 1)
+    assert max(abs(a - b) for a, b in zip(p.target, (2.15, -0.12, 0.0))) < 1e-6
+    assert max(abs(a - b) for a, b in zip(p.eye, (2.15 + 2.5, -0.12 + 4.45, 5.7))) < 1e-5 and abs(p.size - 5.25) < 1e-6
+    assert abs(p.attenuation_distance - 0.18) < 1e-7 and abs(p.surface_roughness - 0.3) < 1e-7
+    tank = waves_gb300.config("tank")  # 16 x 0.05 m = 0.8 m deep in z: the close view
+    lib.waves_render_params_default(C.byref(p), C.byref(tank), 64, 64)
+    assert max(abs(a - b) for a, b in zip(p.target, (3.45, -0.08, 0.0))) < 1e-6 and abs(p.size - 1.5) < 1e-6
