@@ -36,6 +36,31 @@ def tank_jacobi(**kw):
     return tank_small(mg_smoother=0, mg_smoothing=2, mg_maintenance=0, **kw)
 
 
+def tank_periodic(**kw):
+    """The small tank, periodic in x (the periodic-x index, delta and transfer paths)."""
+    return tank_small(periodic_x=1, **kw)
+
+
+def dam_break(**kw):
+    """Fixture 1: a water column released in the 24x16x8 tank (large free-surface motion)."""
+    return wg.config("default", n=(24, 16, 8), shape=1, pressure_tolerance=1e-6, **kw)
+
+
+def jets(**kw):
+    """Fixture 4: two colliding 2 m/s jets (CFL limits, retries)."""
+    return wg.config("default", n=(24, 16, 8), shape=4, pressure_tolerance=1e-6, **kw)
+
+
+def wave_periodic(**kw):
+    """Fixture 5: one second-order Stokes wavelength over a periodic 0.8 m channel."""
+    import math
+    k = 2.0 * math.pi / (32 * 0.025)
+    omega = math.sqrt(9.81 * k * math.tanh(k * 0.45))
+    return wg.config("default", n=(32, 16, 8), shape=5, periodic_x=1, wave=(0.03, k, omega, 0.45),
+                     stokes_second=1, **kw)  # the reference's CG tolerance, 1e-4
+
+
 CASES = {"tank_small": tank_small, "tank_ref_cfl": tank_ref_cfl, "beach_coarse": beach_coarse,
          "beach_slope": beach_slope, "beach_slope_bf16": beach_slope_bf16, "tank_bf16": tank_bf16,
-         "tank_jacobi": tank_jacobi}
+         "tank_jacobi": tank_jacobi, "tank_periodic": tank_periodic, "dam_break": dam_break, "jets": jets,
+         "wave_periodic": wave_periodic}

@@ -212,3 +212,23 @@ def test_history_parity(gpu_lib, name):
     m = first_mismatch(ag[:words].astype(np.int64), ao[:words].astype(np.int64))
     assert not m, f"audit: {m}"
     g.close()
+
+
+@pytest.mark.gpu
+def test_halting_parity(gpu_lib):
+    """A run the algorithm halts: the periodic Stokes wave at CG tolerance 1e-6, whose true residual
+    does not converge within the four defect corrections, fails acceptance (code 4) at the same
+    trial on the GPU and on the oracle, with the same rolled-back state."""
+    from tests.cases import wave_periodic
+    cfg = wave_periodic(pressure_tolerance=1e-6)
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    g.request_steps(STEPS)
+    assert g.run() == 4  # WAVES_SOLVER_FAILED
+    o.request_steps(STEPS)
+    o.run()
+    cg, co = g.control(), o.control()
+    assert cg[7] == co[7] == 4 and cg[2] == co[2] < STEPS
+    problems = compare_state(g, o, cfg, "halted")
+    assert not problems, "\n".join(problems)
+    g.close()
