@@ -60,7 +60,49 @@ def wave_periodic(**kw):
                      stokes_second=1, **kw)  # the reference's CG tolerance, 1e-4
 
 
+def box_pool(**kw):
+    """Fixture 2: a falling block over a shallow pool."""
+    return wg.config("default", n=(24, 16, 8), shape=2, pressure_tolerance=1e-6, **kw)
+
+
+def inflow(**kw):
+    """Fixture 3: a 0.25 m/s current under the surface."""
+    return wg.config("default", n=(24, 16, 8), shape=3, pressure_tolerance=1e-6, **kw)
+
+
+def absorber(**kw):
+    """Fixture 6: the coarse beach with the right-hand absorber."""
+    return beach_coarse(shape=6, **kw)
+
+
+def height_normals(**kw):
+    """The corrugated tank with height-function normals (flag bit 0)."""
+    return tank_small(height_normals=1, **kw)
+
+
+def linear_air(**kw):
+    """A steeper corrugation with the linear air extension."""
+    return tank_small(linear_air=1, corrugation=0.1, **kw)
+
+
+def max_face_cfl(**kw):
+    """The dam break with the CFL rate taken as the maximum over axes."""
+    return dam_break(max_face_cfl=1, **kw)
+
+
+def plain_transport(**kw):
+    """MacCormack without the trace cache and without valid-band advection (flag bits 1, 2 off)."""
+    return tank_small(transport_cache=0, active_advection=0, corrugation=0.1, **kw)
+
+
+def interior_fast(**kw):
+    """MacCormack with the interior sampling fast path (flag bit 3)."""
+    return tank_small(transport_interior=1, corrugation=0.1, **kw)
+
+
 CASES = {"tank_small": tank_small, "tank_ref_cfl": tank_ref_cfl, "beach_coarse": beach_coarse,
          "beach_slope": beach_slope, "beach_slope_bf16": beach_slope_bf16, "tank_bf16": tank_bf16,
          "tank_jacobi": tank_jacobi, "tank_periodic": tank_periodic, "dam_break": dam_break, "jets": jets,
-         "wave_periodic": wave_periodic}
+         "wave_periodic": wave_periodic, "box_pool": box_pool, "inflow": inflow, "absorber": absorber,
+         "height_normals": height_normals, "linear_air": linear_air, "max_face_cfl": max_face_cfl,
+         "plain_transport": plain_transport, "interior_fast": interior_fast}

@@ -631,6 +631,10 @@ DI void finalize_op9(const Dev& D, const double* s) {
   if (isnan(c[13]) || isinf(c[13])) c[7] = 2;
   else if (residual_converged(D, s, c[10])) c[6] = 1;
   else if (c[8] > 4096) c[7] = 3;
+  // The reference runs ipb iterations per batch and every batch starts with op 1, which clears
+  // the set-up flag (pressure_pass.glslinc:20-24); a trial still solving after a whole batch
+  // continues in the next one.
+  if (c[6] < .5 && c[7] < .5 && D.ipb > 0 && (long long)c[8] % D.ipb == 0) c[5] = 0;
 }
 
 

@@ -131,6 +131,7 @@ struct Dev {
   int L;
   MGLevelDev lv[kMaxLevels];
   int mg_smoother, mg_smoothing, mg_mode, mg_lag, mg_aggr;
+  int ipb;                   // CG iterations per reference batch (coupled_gpu.gd:14)
   int bf16;                  // storage precision of the MG vectors/operators
   void* mgv;                 // 8 fields x total_nodes (float or bf16): 0 rhs,1/2 x,3 active,4 scale,6 res,7 cheb d
   long long mg_nodes;        // total nodes over all levels

@@ -270,6 +270,7 @@ waves_status setup_device(waves_handle* h) {
   D.cfl = k.cfl;
   D.cell_d = double(k.spacing[0]) * double(k.spacing[1]) * double(k.spacing[2]);
   D.zone_x_end = coastal_zone_end(k);
+  D.ipb = k.iterations_per_batch;
   D.mg_smoother = k.mg_smoother;
   D.mg_smoothing = k.mg_smoothing;
   D.mg_mode = k.mg_maintenance;
