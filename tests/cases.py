@@ -100,9 +100,25 @@ def interior_fast(**kw):
     return tank_small(transport_interior=1, corrugation=0.1, **kw)
 
 
+def tank_structure(**kw):
+    """The structure-only multigrid maintenance policy (mode 1)."""
+    return tank_small(mg_maintenance=1, **kw)
+
+
+def cheb2(**kw):
+    """Two Chebyshev sweeps per smoothing call."""
+    return tank_small(mg_smoothing=2, **kw)
+
+
+def aggr3(**kw):
+    """Aggregation transfers from level 3 on."""
+    return tank_small(mg_aggregate_from=3, **kw)
+
+
 CASES = {"tank_small": tank_small, "tank_ref_cfl": tank_ref_cfl, "beach_coarse": beach_coarse,
          "beach_slope": beach_slope, "beach_slope_bf16": beach_slope_bf16, "tank_bf16": tank_bf16,
          "tank_jacobi": tank_jacobi, "tank_periodic": tank_periodic, "dam_break": dam_break, "jets": jets,
          "wave_periodic": wave_periodic, "box_pool": box_pool, "inflow": inflow, "absorber": absorber,
          "height_normals": height_normals, "linear_air": linear_air, "max_face_cfl": max_face_cfl,
-         "plain_transport": plain_transport, "interior_fast": interior_fast}
+         "plain_transport": plain_transport, "interior_fast": interior_fast, "tank_structure": tank_structure,
+         "cheb2": cheb2, "aggr3": aggr3}

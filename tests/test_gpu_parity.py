@@ -232,3 +232,23 @@ def test_halting_parity(gpu_lib):
     problems = compare_state(g, o, cfg, "halted")
     assert not problems, "\n".join(problems)
     g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["dam_break", "jets"])
+def test_long_run_parity(gpu_lib, name):
+    """24 accepted steps with rejections, retries and a multigrid rebuild at most trials: the state
+    and the hierarchy audit words agree with the oracle at the end."""
+    cfg = CASES[name]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for s in (g, o):
+        s.request_steps(24)
+        s.run()
+    problems = compare_state(g, o, cfg, "24 steps")
+    assert not problems, "\n".join(problems)
+    assert g.control()[2] == 24 and g.control()[3] > 0  # rejections happened
+    ag, ao = g.history()[2], o.audit()
+    words = 64 + 32 * int(ag[13])
+    assert int(ag[13]) == int(ao[13]) and np.array_equal(ag[:words], ao[:words])
+    g.close()
