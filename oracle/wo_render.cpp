@@ -1,5 +1,5 @@
-// TEST INFRASTRUCTURE ONLY: CPU restatement of the presentation ray-march, the checker of the
-// library's waves_render.  Follows neuron-forest/waves water/presentation/water.gdshader:21-176
+// TEST INFRASTRUCTURE ONLY: CPU restatement of the presentation ray-march, against which the tests
+// compare the library's waves_render.  Follows neuron-forest/waves water/presentation/water.gdshader:21-176
 // (trace_water, normal_weight, optical_normal, fragment), water/presentation/
 // daylight.gdshaderinc:1-16 and water/shaders/render/clay.gdshader:8-66 statement by statement,
 // in FP32 with no contraction (-ffp-contract=off); transcendentals in FP64 rounded to FP32.

@@ -1,7 +1,6 @@
 """Test-side access to the CPU oracle (oracle/libwaves_oracle.so via ctypes).
 
-The oracle is the checker: tests compare the CUDA library against it; nothing in the product
-imports it.  `build()` compiles it with oracle/Makefile when the library is missing or stale.
+Tests compare the CUDA library against the oracle; nothing in the product imports it.  `build()` compiles it with oracle/Makefile when the library is missing or stale.
 """
 import ctypes as C
 import os
