@@ -72,3 +72,25 @@ def test_frame_budget_bounds_trials(gpu_lib):
     with pytest.raises(wg.WavesError):
         s.frame(gpu_budget_ms=0)
     s.close()
+
+
+@pytest.mark.gpu
+def test_gdscript_mirror_frames(gpu_lib):
+    """The CoastalGPU mirror driven the way lab_runner.gd drives coastal_view: request, then one
+    frame() per rendered frame until it reports nothing left; telemetry packets carry the
+    scheduler's keys and the accepted steps reach the quota."""
+    from waves_gb300.gd import CoastalGPU
+    solver = CoastalGPU({"n": (64, 40, 8), "origin": (0.5, -0.6, -0.2), "spacing": (0.025, 0.025, 0.025),
+                         "shape": 7, "slope": 6.0, "wave": (0.08, 2.52502, 4.48799, 0.45)})
+    packets = []
+    solver.connect(packets.append)
+    solver.start()
+    solver.request(4)
+    deadline = time.monotonic() + 300
+    while solver.frame(gpu_budget_ms=5.0) and time.monotonic() < deadline:
+        time.sleep(0.002)
+    assert packets[0].get("initialized") and len(packets) > 2
+    assert max(p.get("queue_depth", 0) for p in packets) <= 3
+    assert packets[-1]["submission_accepted_steps"] == 4 and packets[-1]["failure"] == 0
+    assert packets[-1]["R_fluid"] > 0
+    solver.close()

@@ -12,9 +12,9 @@ water/pressure_gpu.gd, water/coupled_gpu.gd and water/coastal_gpu.gd expose to t
     solver.planes / solver.kinds             # accepted-surface textures (pressure_gpu.gd:4-5)
 
 These classes keep those names and semantics over the C ABI.  `frame()` plays the role of the
-render-thread work of work_scheduler.gd:41-87: it submits trials while the quota is unmet and the
-solver has not halted, then emits one telemetry packet from the control block.  The settings
-dictionary uses the keys of lab_runner.gd:26.
+render-thread work of work_scheduler.gd:41-87: one budgeted submission per call (waves_frame),
+never a wait for the GPU, and one telemetry packet; `run()` submits until the quota is met.  The
+settings dictionary uses the keys of lab_runner.gd:26.
 """
 import math
 
@@ -93,19 +93,26 @@ class PressureGPU:
         assert math.isfinite(seconds) and seconds >= 0
         self._target = -float(seconds)
 
-    def frame(self, max_trials=96):
-        """Submit work toward the current quota (the scheduler's frame), then emit telemetry."""
+    def frame(self, gpu_budget_ms=14.0, max_inflight=3, max_trials=96, cpu_budget_ms=4.0):
+        """One rendered frame of water/work_scheduler.gd:frame through waves_frame: trials toward the
+        current quota within the GPU and CPU budgets, at most max_inflight unfinished submissions,
+        never a wait for the GPU; emits the frame's telemetry (work_scheduler.gd:40,86 keys).
+        Returns False once the quota is met with nothing in flight, or the solver halted."""
         if self.solver is None or self.closed:
-            return
+            return False
         if self._target >= 0:
             self.solver.request_steps(int(self._target))
         else:
             self.solver.request_time(-self._target)
-        st = self.solver.stats()
-        if st["failure"] == 0:
-            self.solver.advance(max_trials)
-        self.last_stats = self.solver.stats()
-        self._emit(self.last_stats)
+        r = self.solver.frame(gpu_budget_ms=gpu_budget_ms, max_inflight=max_inflight, max_trials=max_trials,
+                              cpu_budget_ms=cpu_budget_ms)
+        packet = {"submission_chunks": r["trials_submitted"], "queue_depth": r["queue_depth"],
+                  "predicted_gpu_ns": r["predicted_gpu_ms"] * 1e6, "gpu_ns": r["gpu_ms_total"] * 1e6,
+                  "R_fluid": r["r_fluid"], "submission_accepted_steps": r["accepted_steps"],
+                  "submission_accepted_time": r["accepted_time"], "failure": r["halted"]}
+        self.last_stats.update({"accepted_steps": r["accepted_steps"], "accepted_time": r["accepted_time"]})
+        self._emit(packet)
+        return not (r["idle"] or r["halted"])
 
     def run(self, trials_per_sync=4):
         if self._target >= 0:
