@@ -53,6 +53,8 @@ def lib():
             "wo_mg_state": (None, [vp, C.POINTER(C.c_uint32)]),
             "wo_get_history": (None, [vp, fp, fp]),
             "wo_mg_audit": (None, [vp, C.POINTER(C.c_uint32), C.c_size_t]),
+            "wo_net_gradients": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, fp, C.POINTER(fp),
+                                              C.POINTER(fp), C.POINTER(fp), C.POINTER(fp), fp]),
             "wo_cube_volume": (C.c_float, [C.c_float] * 4),
             "wo_inverse_volume": (C.c_float, [C.c_float] * 4),
             "wo_cube_volume_d": (C.c_double, [C.c_double] * 4),
@@ -198,3 +200,26 @@ def render(planes, kinds, cfg, params, clock_time):
     L.wo_render(planes.ctypes.data_as(fp), kinds.ctypes.data_as(fp), C.byref(cfg), C.byref(params),
                 float(np.float32(clock_time)), img.ctypes.data_as(fp), tr.ctypes.data_as(fp))
     return img, tr
+
+
+NET_CHANNELS = [(3, 16), (16, 16), (16, 16), (16, 1)]
+
+
+def net_gradients(x, target, mask, weights, biases):
+    """The oracle's training step (oracle/wo_net.cpp): loss, per-layer dL/dW [co][27][ci] and dL/db,
+    and the output, for a batch x[b][3][z][y][x] with FP32 weights."""
+    L = lib()
+    fp = C.POINTER(C.c_float)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    B, _, nz, ny, nx = x.shape
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    ws = [np.ascontiguousarray(w, dtype=np.float32) for w in weights]
+    bs = [np.ascontiguousarray(b, dtype=np.float32) for b in biases]
+    gws = [np.zeros_like(w) for w in ws]
+    gbs = [np.zeros_like(b) for b in bs]
+    y = np.zeros((B, nz, ny, nx), dtype=np.float32)
+    arr = lambda lst: (fp * len(lst))(*[a.ctypes.data_as(fp) for a in lst])
+    loss = L.wo_net_gradients(B, nz, ny, nx, x.ctypes.data_as(fp), target.ctypes.data_as(fp), mask.ctypes.data_as(fp),
+                              arr(ws), arr(bs), arr(gws), arr(gbs), y.ctypes.data_as(fp))
+    return loss, gws, gbs, y
