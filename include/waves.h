@@ -302,6 +302,25 @@ typedef struct waves_warm_start_model {
 } waves_warm_start_model;
 waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model* model);
 
+/* Training of the warm-start network on the GPU (own forward, backward and Adam kernels): a batch
+ * of crops with zero padding at the crop edge; inputs, weights and activations rounded to BF16 as
+ * in the inference kernels, FP32 accumulation forward, FP64 in the gradients.  Weights are the FP32
+ * masters [co][27][ci] (tap (kz * 3 + ky) * 3 + kx), biases [co], per layer; all buffers host. */
+typedef struct waves_net_batch {
+  int32_t crops, nz, ny, nx;  /* crop count and size in cells */
+  const float* x;             /* [crops][3][nz][ny][nx]: scaled F, b, p_prev */
+  const float* target;        /* [crops][nz][ny][nx]: the scaled pressure correction */
+  const float* mask;          /* [crops][nz][ny][nx]: 1 where the loss counts */
+} waves_net_batch;
+/* One forward and backward pass: loss = sum mask (y - target)^2 / max(sum mask, 1), dL/dW and dL/db
+ * of every layer, and the output y ([crops][nz][ny][nx], may be NULL). */
+waves_status waves_net_gradients(const waves_net_batch* batch, const float* const* weights, const float* const* bias,
+                                 double* loss, float* const* grad_w, float* const* grad_b, float* y, int32_t device);
+/* `iterations` Adam steps (beta 0.9 / 0.999, eps 1e-8) on the batch; weights and biases updated in
+ * place; the loss before each step in loss_history (may be NULL). */
+waves_status waves_net_train(const waves_net_batch* batch, float* const* weights, float* const* bias, int32_t iterations,
+                             float learning_rate, double* loss_history, int32_t device);
+
 /* Liquid volume sum over cells of F * hx*hy*hz (FP64) of a caller-owned device array F[nx*ny*nz]
  * (x-fastest), written to the caller-owned device double *out, enqueued on `stream` (a
  * cudaStream_t; NULL = default stream).  No counterpart in the reference.  It allocates nothing:

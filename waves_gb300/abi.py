@@ -131,6 +131,18 @@ class WavesWarmStartModel(C.Structure):
     ]
 
 
+class WavesNetBatch(C.Structure):
+    _fields_ = [
+        ("crops", C.c_int32),
+        ("nz", C.c_int32),
+        ("ny", C.c_int32),
+        ("nx", C.c_int32),
+        ("x", C.POINTER(C.c_float)),
+        ("target", C.POINTER(C.c_float)),
+        ("mask", C.POINTER(C.c_float)),
+    ]
+
+
 class WavesRenderParams(C.Structure):
     _fields_ = [
         ("width", C.c_int32),
@@ -228,6 +240,8 @@ WAVES_ABI_SYMBOLS = [
     "waves_save",
     "waves_load",
     "waves_set_warm_start",
+    "waves_net_gradients",
+    "waves_net_train",
     "waves_last_error",
     "waves_liquid_volume_noalloc",
 ]
@@ -272,6 +286,10 @@ def declare(lib):
         "waves_save": (C.c_int, [h, C.c_void_p, P(C.c_size_t)]),
         "waves_load": (C.c_int, [h, C.c_void_p, C.c_size_t]),
         "waves_set_warm_start": (C.c_int, [h, P(WavesWarmStartModel)]),
+        "waves_net_gradients": (C.c_int, [P(WavesNetBatch), P(P(C.c_float)), P(P(C.c_float)), P(C.c_double),
+                                          P(P(C.c_float)), P(P(C.c_float)), P(C.c_float), C.c_int32]),
+        "waves_net_train": (C.c_int, [P(WavesNetBatch), P(P(C.c_float)), P(P(C.c_float)), C.c_int32, C.c_float,
+                                      P(C.c_double), C.c_int32]),
         "waves_last_error": (C.c_char_p, [h]),
         "waves_liquid_volume_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                                   C.c_float, C.c_void_p, C.c_void_p]),

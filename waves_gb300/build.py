@@ -17,7 +17,7 @@ LIB = os.path.join(OUT, "libwaves_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["waves_abi.cu", "k_pcg.cu", "k_motion.cu", "k_geom.cu", "k_mg.cu", "k_init.cu", "k_net.cu", "k_render.cu", "noalloc.cu", "config.cpp"]
+SOURCES = ["waves_abi.cu", "k_pcg.cu", "k_motion.cu", "k_geom.cu", "k_mg.cu", "k_init.cu", "k_net.cu", "k_train.cu", "k_render.cu", "noalloc.cu", "config.cpp"]
 
 
 def nvcc():

@@ -1,9 +1,12 @@
 """Learned warm start: solve-pair capture, training and evaluation (waves_gb300.learned.train).
 
 The network itself runs in the library (k_net.cu, waves_set_warm_start); this package produces
-its weights.  Training is offline and uses PyTorch on the GPU; the exported model is the BF16
-weight layout of include/waves.h.
+its weights, either with the library's own training kernels (k_train.cu: waves_net_gradients,
+waves_net_train, wrapped below) or with PyTorch; the exported model is the BF16 weight layout of
+include/waves.h.
 """
+import ctypes as C
+
 import numpy as np
 
 CHANNELS = [(3, 16), (16, 16), (16, 16), (16, 1)]
@@ -21,3 +24,55 @@ def load_model(path):
     weights = [z[f"w{l}"] for l in range(len(CHANNELS))]
     biases = [z[f"b{l}"] for l in range(len(CHANNELS))]
     return weights, biases, tuple(float(v) for v in z["input_scale"]), float(z["output_scale"])
+
+
+def _batch(x, target, mask):
+    from waves_gb300.abi import WavesNetBatch
+    fp = C.POINTER(C.c_float)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    B, ch, nz, ny, nx = x.shape
+    assert ch == 3 and target.shape == (B, nz, ny, nx) and mask.shape == target.shape
+    bt = WavesNetBatch(B, nz, ny, nx, x.ctypes.data_as(fp), target.ctypes.data_as(fp), mask.ctypes.data_as(fp))
+    return bt, (x, target, mask)
+
+
+def _ptrs(arrays):
+    fp = C.POINTER(C.c_float)
+    return (fp * len(arrays))(*[a.ctypes.data_as(fp) for a in arrays])
+
+
+def net_gradients(x, target, mask, weights, biases, device=0):
+    """One forward and backward pass on the GPU (waves_net_gradients): (loss, dL/dW per layer
+    [co][27][ci], dL/db per layer, output y)."""
+    import waves_gb300 as wg
+    lib = wg.load()
+    bt, keep = _batch(x, target, mask)
+    ws = [np.ascontiguousarray(w, dtype=np.float32).reshape(co, 27, ci) for w, (ci, co) in zip(weights, CHANNELS)]
+    bs = [np.ascontiguousarray(b, dtype=np.float32) for b in biases]
+    gws = [np.zeros_like(w) for w in ws]
+    gbs = [np.zeros_like(b) for b in bs]
+    y = np.zeros(keep[1].shape, dtype=np.float32)
+    loss = C.c_double()
+    st = lib.waves_net_gradients(C.byref(bt), _ptrs(ws), _ptrs(bs), C.byref(loss), _ptrs(gws), _ptrs(gbs),
+                                 y.ctypes.data_as(C.POINTER(C.c_float)), int(device))
+    if st != 0:
+        raise wg.WavesError(f"waves_net_gradients: status {st}")
+    return loss.value, gws, gbs, y
+
+
+def net_train(x, target, mask, weights, biases, iterations, learning_rate, device=0):
+    """`iterations` Adam steps on the GPU (waves_net_train) from FP32 weights [co][27][ci] and biases;
+    returns (weights, biases, loss per step)."""
+    import waves_gb300 as wg
+    lib = wg.load()
+    bt, keep = _batch(x, target, mask)
+    ws = [np.array(w, dtype=np.float32).reshape(co, 27, ci) for w, (ci, co) in zip(weights, CHANNELS)]
+    bs = [np.array(b, dtype=np.float32) for b in biases]
+    hist = np.zeros(max(int(iterations), 1), dtype=np.float64)
+    st = lib.waves_net_train(C.byref(bt), _ptrs(ws), _ptrs(bs), int(iterations), float(learning_rate),
+                             hist.ctypes.data_as(C.POINTER(C.c_double)), int(device))
+    if st != 0:
+        raise wg.WavesError(f"waves_net_train: status {st}")
+    return ws, bs, hist[:int(iterations)]

@@ -1,6 +1,6 @@
 """Train the warm-start network on solve pairs captured from the solver, export it, evaluate it.
 
-    python -m waves_gb300.learned.train --seeds 8 --pairs 40 --out model.npz [--eval-seeds 2]
+    python -m waves_gb300.learned.train --seeds 8 --pairs 40 --out model.npz [--eval-seeds 2] [--trainer torch]
 
 Capture: for each seed the 310x48x80 beach (the lab settings) runs with a wave amplitude drawn
 from U(0.04, 0.10) m and a period from U(1.2, 1.8) s (wavenumber by the same dispersion
@@ -9,7 +9,9 @@ advances in the CUDA-graph path to the sampling times and takes one trial throug
 host-driven phases of include/waves_debug.h: after op 2 the candidate F and p_prev, after the CG
 set-up b, and at the first round's convergence (relative residual 1e-6) p*.
 
-Training (PyTorch, offline): the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
+Training, --trainer cuda (default): the library's own kernels (k_train.cu, waves_net_train) run
+full-batch Adam on a fixed set of random crops with the MSE objective below.  --trainer torch:
+PyTorch, offline: the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
 ReLU, zero padding) maps (F, b * s_b, p_prev * s_p) to (p* - p_prev) / s_out on wet cells, with
 s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data.  The
 default objective is the initial residual the solver will see, |r0 - A (s_out y)|^2 / |r0|^2 over
@@ -193,6 +195,50 @@ def train(pairs, n, steps, seed, device, objective="residual"):
     return weights, biases, (1.0, s_b, s_p), s_out, resid / max(total, 1e-30)
 
 
+def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e-3):
+    """The MSE objective trained with the library's own kernels (waves_net_train: forward, backward
+    and Adam on the GPU): a fixed batch of random crops of the training pairs, the loss counted on
+    wet cells at least `edge` cells from the crop edge; full-batch Adam for `steps` steps."""
+    from waves_gb300.learned import net_gradients, net_train
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    grid = lambda a: np.asarray(a, dtype=np.float32).reshape(nz, ny, nx)
+    wet = [grid(p["kind"]) > 0 for p in pairs]
+    allw = np.concatenate([w.ravel() for w in wet])
+    b_all = np.concatenate([grid(p["b"]).ravel() for p in pairs])[allw]
+    pp_all = np.concatenate([grid(p["p_prev"]).ravel() for p in pairs])[allw]
+    dp_all = np.concatenate([(grid(p["p_star"]) - grid(p["p_prev"])).ravel() for p in pairs])[allw]
+    s_b = 1.0 / max(float(b_all.std()), 1e-12)
+    s_p = 1.0 / max(float(pp_all.std()), 1e-12)
+    s_out = max(float(dp_all.std()), 1e-12)
+    cx, cy, cz = min(crop[0], nx), min(crop[1], ny), min(crop[2], nz)
+    xs = np.zeros((crops, 3, cz, cy, cx), np.float32)
+    ys = np.zeros((crops, cz, cy, cx), np.float32)
+    ms = np.zeros((crops, cz, cy, cx), np.float32)
+    inner = np.zeros((cz, cy, cx), np.float32)
+    inner[edge:cz - edge, edge:cy - edge, edge:cx - edge] = 1.0
+    for k in range(crops):
+        i = int(rng.integers(len(pairs)))
+        ox, oy, oz = int(rng.integers(nx - cx + 1)), int(rng.integers(ny - cy + 1)), int(rng.integers(nz - cz + 1))
+        sl = (slice(oz, oz + cz), slice(oy, oy + cy), slice(ox, ox + cx))
+        p = pairs[i]
+        xs[k, 0] = grid(p["F"])[sl]
+        xs[k, 1] = grid(p["b"])[sl] * s_b
+        xs[k, 2] = grid(p["p_prev"])[sl] * s_p
+        ys[k] = (grid(p["p_star"])[sl] - grid(p["p_prev"])[sl]) / s_out
+        ms[k] = wet[i][sl] * inner
+    weights = [rng.normal(0.0, 1.0 / np.sqrt(27 * ci), size=(co, 27, ci)).astype(np.float32) * (0.1 if co == 1 else 1.0)
+               for ci, co in CHANNELS]
+    biases = [np.zeros(co, np.float32) for _, co in CHANNELS]
+    t0 = time.time()
+    weights, biases, hist = net_train(xs, ys, ms, weights, biases, steps, lr)
+    print(f"cuda trainer: masked MSE {hist[0]:.4e} -> {hist[-1]:.4e} in {steps} steps ({time.time() - t0:.1f} s)", flush=True)
+    total = float((ms * ys * ys).sum() / max(ms.sum(), 1.0))
+    left, _, _, _ = net_gradients(xs, ys, ms, weights, biases)
+    bits = [bf16_bits(w) for w in weights]
+    return bits, biases, (1.0, s_b, s_p), s_out, left / max(total, 1e-30)
+
+
 def evaluate(path, seeds, steps):
     weights, biases, iscale, oscale = load_model(path)
     rows = []
@@ -233,16 +279,23 @@ def main():
     ap.add_argument("--eval-steps", type=int, default=120)
     ap.add_argument("--out", default="model.npz")
     ap.add_argument("--objective", default="residual", choices=["residual", "mse"])
+    ap.add_argument("--trainer", default="cuda", choices=["cuda", "torch"],
+                    help="cuda: the library's own training kernels (MSE objective); torch: PyTorch")
+    ap.add_argument("--crops", type=int, default=32)
     args = ap.parse_args()
-    import torch
-    device = "cuda" if torch.cuda.is_available() else "cpu"
     cfg, _, _ = beach(1)
     pairs = capture(range(1, args.seeds + 1), args.pairs, args.t0, args.gap)
-    weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device, args.objective)
+    if args.trainer == "cuda":
+        args.objective = "mse"
+        weights, biases, iscale, oscale, unexplained = train_cuda(pairs, tuple(cfg.n), args.steps, 0, args.crops)
+    else:
+        import torch
+        device = "cuda" if torch.cuda.is_available() else "cpu"
+        weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device, args.objective)
     np.savez(args.out, **{f"w{l}": w for l, w in enumerate(weights)}, **{f"b{l}": b for l, b in enumerate(biases)},
              input_scale=np.array(iscale, np.float32), output_scale=np.float32(oscale),
              pairs=len(pairs), seeds=args.seeds, unexplained=unexplained)
-    print(json.dumps({"pairs": len(pairs), "objective": args.objective, "fraction_left": unexplained, "input_scale": iscale,
+    print(json.dumps({"pairs": len(pairs), "trainer": args.trainer, "objective": args.objective, "fraction_left": unexplained, "input_scale": iscale,
                       "output_scale": oscale, "out": args.out}), flush=True)
     if args.eval_seeds > 0:
         evaluate(args.out, range(101, 101 + args.eval_seeds), args.eval_steps)
