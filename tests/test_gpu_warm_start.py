@@ -99,3 +99,40 @@ def test_solver_with_network_stays_within_fp64_bars(gpu_lib):
         Fo = split(o.bank_d(), tuple(cfg.n))[0]
         assert np.max(np.abs(Fg - Fo)) <= F_TOLERANCE
     print(f"warm start used in {g.stats()['warm_start_used']} of {int(g.control()[32])} trials")
+
+
+@pytest.mark.gpu
+def test_trained_network_gain_over_plain_mgpcg(gpu_lib):
+    """What the shipped network (waves_gb300/learned/model_beach.npz) gains on a held-out beach
+    (seed 101 of the capture's amplitude/period draws, 60 steps from t = 1 s, CG relres 1e-6):
+    the same run with and without it.  The residual guard only takes the network where its
+    initial residual is smaller, so it must not cost CG iterations; the gain is reported.
+    Measured on a GB300: in these 60 steps the network is taken in 0 of 60 trials (13.78
+    iterations per step both ways); over 120 steps, in 34 of 120 (14.24 against 14.35)."""
+    import os
+    from waves_gb300.learned import load_model
+    from waves_gb300.learned.train import beach
+
+    path = os.path.join(os.path.dirname(wg.__file__), "learned", "model_beach.npz")
+    weights, biases, iscale, oscale = load_model(path)
+    steps, out = 60, {}
+    for warm in (0, 1):
+        cfg, _, _ = beach(101, warm)
+        s = wg.WavesSolver(cfg)
+        if warm:
+            s.set_warm_start(weights, biases, iscale, oscale)
+        s.request_time(1.0)
+        s.run()
+        c0 = s.control()
+        s.request_steps(int(c0[2]) + steps)
+        s.run()
+        c1 = s.control()
+        assert c1[2] == c0[2] + steps and s.stats()["failure"] == 0
+        out[warm] = ((c1[18] - c0[18]) / steps, int(c1[102] - c0[102]), int(c1[32] - c0[32]))
+        s.close()
+    (plain, _, _), (learned, used, trials) = out[0], out[1]
+    print(f"plain {plain:.2f} it/step, learned {learned:.2f} it/step, network taken in {used} of {trials} trials")
+    assert 0 <= used <= trials
+    if used == 0:
+        assert learned == plain  # never taken: the run is the plain run, bit for bit
+    assert learned <= plain + 0.5
