@@ -304,13 +304,22 @@ waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model*
 
 /* Training of the warm-start network on the GPU (own forward, backward and Adam kernels): a batch
  * of crops with zero padding at the crop edge; inputs, weights and activations rounded to BF16 as
- * in the inference kernels, FP32 accumulation forward, FP64 in the gradients.  Weights are the FP32
- * masters [co][27][ci] (tap (kz * 3 + ky) * 3 + kx), biases [co], per layer; all buffers host. */
+ * in the inference kernels.  Weights are the FP32 masters [co][27][ci] (tap (kz * 3 + ky) * 3 + kx),
+ * biases [co], per layer; all buffers host.  Two arithmetics:
+ *   WAVES_NET_EXACT   FP32 accumulation forward in a fixed order (the CPU oracle's), FP64 sums in
+ *                     the weight and input gradients, gradients passed through the roundings in FP32;
+ *   WAVES_NET_TENSOR  implicit GEMM on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
+ *                     accumulation) for the forward pass, the input gradients and the weight
+ *                     gradients; the gradients between layers are BF16 operands, the weight
+ *                     gradients' per-block partials are summed in FP64 in a fixed order. */
+#define WAVES_NET_EXACT 0
+#define WAVES_NET_TENSOR 1
 typedef struct waves_net_batch {
   int32_t crops, nz, ny, nx;  /* crop count and size in cells */
   const float* x;             /* [crops][3][nz][ny][nx]: scaled F, b, p_prev */
   const float* target;        /* [crops][nz][ny][nx]: the scaled pressure correction */
   const float* mask;          /* [crops][nz][ny][nx]: 1 where the loss counts */
+  int32_t arithmetic;         /* WAVES_NET_EXACT or WAVES_NET_TENSOR */
 } waves_net_batch;
 /* One forward and backward pass: loss = sum mask (y - target)^2 / max(sum mask, 1), dL/dW and dL/db
  * of every layer, and the output y ([crops][nz][ny][nx], may be NULL). */

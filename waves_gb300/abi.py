@@ -8,6 +8,8 @@ import ctypes as C
 WAVES_CONTROL_SIZE = 128
 WAVES_NET_LAYERS = 4
 WAVES_NET_HIDDEN = 16
+WAVES_NET_EXACT = 0
+WAVES_NET_TENSOR = 1
 
 STATUS = {
     0: "WAVES_OK",
@@ -140,6 +142,7 @@ class WavesNetBatch(C.Structure):
         ("x", C.POINTER(C.c_float)),
         ("target", C.POINTER(C.c_float)),
         ("mask", C.POINTER(C.c_float)),
+        ("arithmetic", C.c_int32),
     ]
 
 

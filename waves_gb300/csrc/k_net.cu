@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "mma_bf16.cuh"
 
 namespace wg {
 
@@ -25,22 +26,6 @@ constexpr int kStride = 24;                    // bf16 per staged cell (16 chann
 constexpr int kHalo = HX * HY * HZ;
 
 DI bool warm_on(const Dev& D) { return D.c[kNetLoaded] > .5 && D.c[5] > .5 && D.c[7] < .5; }
-
-DI void ldmatrix_x4(uint32_t& a0, uint32_t& a1, uint32_t& a2, uint32_t& a3, const void* smem_row) {
-  const unsigned addr = (unsigned)__cvta_generic_to_shared(smem_row);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-               : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
-               : "r"(addr));
-}
-DI void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1) {
-  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-DI uint32_t pack_bf16(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t*>(&v);
-}
 
 // One layer.  LAYER 0 reads (F, b, p_prev) scaled by input_scale (channels 3..15 zero); layers 1
 // and 2 read the previous BF16 activations; layer 3 (one output channel, one n-tile) writes p_net.

@@ -26,15 +26,16 @@ def load_model(path):
     return weights, biases, tuple(float(v) for v in z["input_scale"]), float(z["output_scale"])
 
 
-def _batch(x, target, mask):
-    from waves_gb300.abi import WavesNetBatch
+def _batch(x, target, mask, tensor):
+    from waves_gb300.abi import WAVES_NET_EXACT, WAVES_NET_TENSOR, WavesNetBatch
     fp = C.POINTER(C.c_float)
     x = np.ascontiguousarray(x, dtype=np.float32)
     target = np.ascontiguousarray(target, dtype=np.float32)
     mask = np.ascontiguousarray(mask, dtype=np.float32)
     B, ch, nz, ny, nx = x.shape
     assert ch == 3 and target.shape == (B, nz, ny, nx) and mask.shape == target.shape
-    bt = WavesNetBatch(B, nz, ny, nx, x.ctypes.data_as(fp), target.ctypes.data_as(fp), mask.ctypes.data_as(fp))
+    bt = WavesNetBatch(B, nz, ny, nx, x.ctypes.data_as(fp), target.ctypes.data_as(fp), mask.ctypes.data_as(fp),
+                       WAVES_NET_TENSOR if tensor else WAVES_NET_EXACT)
     return bt, (x, target, mask)
 
 
@@ -43,12 +44,13 @@ def _ptrs(arrays):
     return (fp * len(arrays))(*[a.ctypes.data_as(fp) for a in arrays])
 
 
-def net_gradients(x, target, mask, weights, biases, device=0):
+def net_gradients(x, target, mask, weights, biases, device=0, tensor=False):
     """One forward and backward pass on the GPU (waves_net_gradients): (loss, dL/dW per layer
-    [co][27][ci], dL/db per layer, output y)."""
+    [co][27][ci], dL/db per layer, output y).  tensor: the tensor-core arithmetic
+    (WAVES_NET_TENSOR) instead of the oracle's order (WAVES_NET_EXACT)."""
     import waves_gb300 as wg
     lib = wg.load()
-    bt, keep = _batch(x, target, mask)
+    bt, keep = _batch(x, target, mask, tensor)
     ws = [np.ascontiguousarray(w, dtype=np.float32).reshape(co, 27, ci) for w, (ci, co) in zip(weights, CHANNELS)]
     bs = [np.ascontiguousarray(b, dtype=np.float32) for b in biases]
     gws = [np.zeros_like(w) for w in ws]
@@ -62,12 +64,12 @@ def net_gradients(x, target, mask, weights, biases, device=0):
     return loss.value, gws, gbs, y
 
 
-def net_train(x, target, mask, weights, biases, iterations, learning_rate, device=0):
+def net_train(x, target, mask, weights, biases, iterations, learning_rate, device=0, tensor=False):
     """`iterations` Adam steps on the GPU (waves_net_train) from FP32 weights [co][27][ci] and biases;
-    returns (weights, biases, loss per step)."""
+    returns (weights, biases, loss per step).  tensor: as in net_gradients."""
     import waves_gb300 as wg
     lib = wg.load()
-    bt, keep = _batch(x, target, mask)
+    bt, keep = _batch(x, target, mask, tensor)
     ws = [np.array(w, dtype=np.float32).reshape(co, 27, ci) for w, (ci, co) in zip(weights, CHANNELS)]
     bs = [np.array(b, dtype=np.float32) for b in biases]
     hist = np.zeros(max(int(iterations), 1), dtype=np.float64)

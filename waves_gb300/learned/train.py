@@ -10,7 +10,8 @@ host-driven phases of include/waves_debug.h: after op 2 the candidate F and p_pr
 set-up b, and at the first round's convergence (relative residual 1e-6) p*.
 
 Training, --trainer cuda (default): the library's own kernels (k_train.cu, waves_net_train) run
-full-batch Adam on a fixed set of random crops with the MSE objective below.  --trainer torch:
+full-batch Adam on a fixed set of random crops with the MSE objective below, as implicit GEMMs on
+the tensor cores (--arithmetic tensor, default) or in the oracle's FP32/FP64 order (exact).  --trainer torch:
 PyTorch, offline: the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
 ReLU, zero padding) maps (F, b * s_b, p_prev * s_p) to (p* - p_prev) / s_out on wet cells, with
 s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data.  The
@@ -195,10 +196,11 @@ def train(pairs, n, steps, seed, device, objective="residual"):
     return weights, biases, (1.0, s_b, s_p), s_out, resid / max(total, 1e-30)
 
 
-def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e-3):
+def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e-3, tensor=True):
     """The MSE objective trained with the library's own kernels (waves_net_train: forward, backward
     and Adam on the GPU): a fixed batch of random crops of the training pairs, the loss counted on
-    wet cells at least `edge` cells from the crop edge; full-batch Adam for `steps` steps."""
+    wet cells at least `edge` cells from the crop edge; full-batch Adam for `steps` steps.  tensor:
+    the tensor-core arithmetic (WAVES_NET_TENSOR), else the oracle's (WAVES_NET_EXACT)."""
     from waves_gb300.learned import net_gradients, net_train
     nx, ny, nz = n
     rng = np.random.default_rng(seed)
@@ -231,8 +233,8 @@ def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e
                for ci, co in CHANNELS]
     biases = [np.zeros(co, np.float32) for _, co in CHANNELS]
     t0 = time.time()
-    weights, biases, hist = net_train(xs, ys, ms, weights, biases, steps, lr)
-    print(f"cuda trainer: masked MSE {hist[0]:.4e} -> {hist[-1]:.4e} in {steps} steps ({time.time() - t0:.1f} s)", flush=True)
+    weights, biases, hist = net_train(xs, ys, ms, weights, biases, steps, lr, tensor=tensor)
+    print(f"cuda trainer ({'tensor' if tensor else 'exact'}): masked MSE {hist[0]:.4e} -> {hist[-1]:.4e} in {steps} steps ({time.time() - t0:.1f} s)", flush=True)
     total = float((ms * ys * ys).sum() / max(ms.sum(), 1.0))
     left, _, _, _ = net_gradients(xs, ys, ms, weights, biases)
     bits = [bf16_bits(w) for w in weights]
@@ -282,12 +284,15 @@ def main():
     ap.add_argument("--trainer", default="cuda", choices=["cuda", "torch"],
                     help="cuda: the library's own training kernels (MSE objective); torch: PyTorch")
     ap.add_argument("--crops", type=int, default=32)
+    ap.add_argument("--arithmetic", default="tensor", choices=["tensor", "exact"],
+                    help="--trainer cuda: tensor-core implicit GEMM (tensor) or the oracle's order (exact)")
     args = ap.parse_args()
     cfg, _, _ = beach(1)
     pairs = capture(range(1, args.seeds + 1), args.pairs, args.t0, args.gap)
     if args.trainer == "cuda":
         args.objective = "mse"
-        weights, biases, iscale, oscale, unexplained = train_cuda(pairs, tuple(cfg.n), args.steps, 0, args.crops)
+        weights, biases, iscale, oscale, unexplained = train_cuda(pairs, tuple(cfg.n), args.steps, 0, args.crops,
+                                                                          tensor=args.arithmetic == "tensor")
     else:
         import torch
         device = "cuda" if torch.cuda.is_available() else "cpu"
