@@ -11,8 +11,8 @@ set-up b, and at the first round's convergence (relative residual 1e-6) p*.
 
 Training, --trainer cuda (default): the library's own kernels (k_train.cu, waves_net_train) run
 full-batch Adam on a fixed set of random crops with the MSE objective below, as implicit GEMMs on
-the tensor cores (--arithmetic tensor, default) or in the oracle's FP32/FP64 order (exact).  --trainer torch:
-PyTorch, offline: the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
+the tensor cores (--arithmetic tensor, default) or in the oracle's FP32/FP64 order (exact).
+--trainer torch: PyTorch, offline: the network of k_net.cu (3x3x3 convolutions 3 -> 16 -> 16 -> 16 -> 1,
 ReLU, zero padding) maps (F, b * s_b, p_prev * s_p) to (p* - p_prev) / s_out on wet cells, with
 s_b, s_p, s_out the inverse standard deviations / standard deviation of the training data.  The
 default objective is the initial residual the solver will see, |r0 - A (s_out y)|^2 / |r0|^2 over
