@@ -183,6 +183,7 @@ def run_ours(args, world, rank, local):
         "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
         "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
         "probes": probes if probe_trials else [],
+        "plan": wg.mg_plan(cfg),
     }
     # e2e: frames through the public API with host buffers, from the state the timed steps started
     # from (checkpoint restored), over the same simulated window unless --e2e-frames says otherwise
@@ -279,6 +280,41 @@ def roofline(probes):
             "timing": "CUDA events on the solver stream around each launch, one host-scheduled trial after the timed steps"}, table
 
 
+STEP_BYTES_FORMULA = ("152 N + builds/step * (28 N + sum_{l>=1} S_l n_l b_m) + CG iterations/step * "
+                      "(72 N + sum_l [7 n_l (S_l b_m + 5 b_v) + 3 n_l b_v] + 8 n_c^2)")
+
+
+def step_bytes_model(plan, iters_per_step, builds_per_step, bf16):
+    """Algorithmic (compulsory) HBM bytes of one accepted step: each distinct array read once and
+    each output written once at its storage precision, halos and cache re-reads excluded.  N = fine
+    cells; per step the non-CG passes move 152 N (VOF sweeps 36 N, MacCormack 24 N, geometry and
+    coefficients 40 N, projection set-up 16 N, gradient, extension and acceptance 36 N); a Galerkin
+    rebuild reads the fine coefficients (28 N) and writes every coarse operator (S_l n_l b_m); a CG
+    iteration moves 72 N outside the preconditioner (matvec 36 N, x and r updates 24 N, direction
+    12 N) plus one V-cycle, per level 7 passes over the operator and 5 vectors and 3 over one vector,
+    and the dense coarse factor (FP32, 2 reads of n_c^2).  b_m = b_v = 4 bytes (FP32 multigrid) or 2
+    (BF16).  plan: waves_gb300.mg_plan(cfg)."""
+    bm = bv = 2 if bf16 else 4
+    n = [l["n"][0] * l["n"][1] * l["n"][2] for l in plan]
+    N = n[0]
+    vcycle = sum(7 * n_l * (l["stencil"] * bm + 5 * bv) + 3 * n_l * bv for n_l, l in zip(n, plan)) + 2 * 4 * n[-1] ** 2
+    rebuild = 28 * N + sum(l["stencil"] * n_l * bm for n_l, l in zip(n[1:], plan[1:]))
+    total = 152 * N + builds_per_step * rebuild + iters_per_step * (72 * N + vcycle)
+    return {"bytes_per_step": total, "non_cg": 152 * N, "rebuild": rebuild, "cg_iteration": 72 * N + vcycle,
+            "vcycle": vcycle, "cells": N}
+
+
+def step_roofline(plan, iters_per_step, builds_per_step, bf16, ms_per_step):
+    """The whole step against the HBM roofline: step_bytes_model bytes / device time per step."""
+    model = step_bytes_model(plan, iters_per_step, builds_per_step, bf16)
+    peak, source = measured_peaks()
+    achieved = model["bytes_per_step"] / (ms_per_step / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{source} copy bandwidth (hbm_gbs)", "bytes_per_step": model["bytes_per_step"],
+            "cg_iteration_bytes": model["cg_iteration"], "rebuild_bytes": model["rebuild"],
+            "non_cg_bytes": model["non_cg"], "formula": STEP_BYTES_FORMULA}
+
+
 def cpu_baseline(args, cfg_mg, seconds):
     """The oracle (CPU restatement, FP32, all host threads) on the beach for a bounded sample."""
     from tests.oracle_ref import Oracle
@@ -360,6 +396,8 @@ def main():
     }
     roof, kernels = roofline(res["probes"])
     line["roofline"] = roof
+    line["step_roofline"] = step_roofline(res["plan"], res["iters"] / steps, res["mg_builds"] / steps,
+                                          args.mg == 16, line["ms_per_step"]) if line["ms_per_step"] > 0 else None
     line["probed_kernels"] = kernels
     every = [p for p in res["probes"] if p["kernel"] == "all"]
     if every and res["trials"]:

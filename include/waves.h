@@ -16,6 +16,8 @@
  *
  * Threading: a handle is used by one thread at a time, except waves_request_steps /
  * waves_request_time, which may be called from any thread (the quota is an atomic).
+ * Device: a call on a handle makes the handle's device current on the calling thread (the training
+ * calls, the device they are given) and leaves it current.
  * Errors never abort the process: every call returns a waves_status; solver failures are the
  * reference's codes in waves_stats_t.failure.
  */
@@ -153,6 +155,11 @@ void waves_config_beach(waves_config* cfg);
 void waves_config_tank(waves_config* cfg);
 /* k solving omega^2 = g k tanh(k h) by 80 bisection steps on [0, 100] (lab_runner.gd:19-25). */
 double waves_dispersion_k(double period_s, double depth_m);
+/* The multigrid level plan that waves_create builds for cfg (pressure_multigrid.gd:37-69, coarse
+ * stencils by _basis/_coarse_stencil :181-198), without a device: *levels = the level count, and for
+ * each of the first `capacity` levels 8 ints in out: nx, ny, nz, the coarsening factors fx, fy, fz
+ * towards the next level, the operator's stencil size, 1 if its transfer is an aggregation. */
+waves_status waves_mg_plan(const waves_config* cfg, int32_t* out, int32_t capacity, int32_t* levels);
 
 /* pressure_gpu.gd _init + start + _initialize: allocates everything on cfg->device, builds the
  * multigrid level plan, runs the initial commands (coupled_gpu.gd:34-37, coastal_gpu.gd:26-27).

@@ -1,5 +1,5 @@
-"""Host-side logic without a GPU: the settings mapping of the GDScript mirror and the bench's
-roofline arithmetic."""
+"""Host-side logic without a GPU: the settings mapping of the GDScript mirror, the multigrid level
+plan (waves_mg_plan), and the bench's roofline arithmetic and step byte model."""
 import importlib.util
 import os
 
@@ -47,3 +47,44 @@ def test_bench_roofline_picks_the_largest_probed_time():
     assert roof["frac"] == pytest.approx(roof["achieved"] / peak)
     assert sum(t["share_of_probed"] for t in table) == pytest.approx(1.0)
     assert bench.roofline([]) == (None, [])
+
+
+def test_mg_plan_of_the_beach_and_the_large_grid():
+    """waves_mg_plan (no device): the level plan of pressure_multigrid.gd:37-69 for the 310x48x80
+    beach (x and y halved first, z kept at hz = 2 hx; aggregation from level 2) and the 620x96x160
+    grid (8 levels), with the Galerkin stencil sizes 7 / 39 / 125 / 27."""
+    wg.load(build_if_missing=True)
+    plan = wg.mg_plan(wg.config("beach"))
+    assert [l["n"] for l in plan] == [(310, 48, 80), (155, 24, 80), (78, 12, 40), (39, 6, 20), (20, 3, 10),
+                                      (10, 2, 5), (5, 2, 5)]
+    assert [l["stencil"] for l in plan] == [7, 39, 125, 27, 27, 27, 27]
+    assert [l["aggregate"] for l in plan] == [False, False] + [True] * 5
+    assert plan[0]["f"] == (2, 2, 1) and plan[1]["f"] == (2, 2, 2)
+    large = wg.mg_plan(wg.config("beach", n=[620, 96, 160], spacing=[0.0125, 0.0125, 0.025]))
+    assert len(large) == 8 and large[0]["n"] == (620, 96, 160) and large[2]["n"] == (155, 24, 80)
+    bad = wg.config("beach", n=[0, 48, 80])
+    with pytest.raises(wg.WavesError):
+        wg.mg_plan(bad)
+
+
+def test_step_bytes_model_reproduces_the_algorithmic_byte_table():
+    """The compulsory-traffic model of one accepted step at the beach: non-CG 152 N = 180.9 MB, one
+    FP32 V-cycle 926 MB (778 N), BF16 half of the operator and vector bytes (463 MB), a CG iteration
+    72 N + V; the 620x96x160 grid's FP32 V-cycle 7.40 GB."""
+    bench = load_bench()
+    wg.load(build_if_missing=True)
+    plan = wg.mg_plan(wg.config("beach"))
+    N = 310 * 48 * 80
+    m32 = bench.step_bytes_model(plan, 0.0, 0.0, False)
+    m16 = bench.step_bytes_model(plan, 0.0, 0.0, True)
+    assert m32["cells"] == N and m32["bytes_per_step"] == 152 * N == pytest.approx(180.9e6, rel=1e-3)
+    assert m32["vcycle"] == pytest.approx(926.2e6, rel=1e-3) and round(m32["vcycle"] / N) == 778
+    assert m16["vcycle"] == pytest.approx(463.1e6, rel=2e-3)
+    assert m32["cg_iteration"] == 72 * N + m32["vcycle"]
+    step = bench.step_bytes_model(plan, 14.0, 0.5, False)
+    assert step["bytes_per_step"] == 152 * N + 0.5 * m32["rebuild"] + 14.0 * m32["cg_iteration"]
+    large = wg.mg_plan(wg.config("beach", n=[620, 96, 160], spacing=[0.0125, 0.0125, 0.025]))
+    assert bench.step_bytes_model(large, 0.0, 0.0, False)["vcycle"] == pytest.approx(7.40e9, rel=2e-3)
+    roof = bench.step_roofline(plan, 14.0, 0.5, False, 12.5)
+    assert roof["achieved"] == pytest.approx(step["bytes_per_step"] / 12.5e-3 / 1e9)
+    assert roof["frac"] == pytest.approx(roof["achieved"] / bench.measured_peaks()[0])

@@ -64,6 +64,18 @@ def dispersion_k(period_s, depth_m):
     return load().waves_dispersion_k(period_s, depth_m)
 
 
+def mg_plan(cfg):
+    """The multigrid level plan waves_create builds for cfg (waves_mg_plan, no device needed): per
+    level its size n, coarsening factors f, stencil size and whether its transfer aggregates."""
+    lib = load()
+    count = C.c_int32()
+    _check(lib, lib.waves_mg_plan(C.byref(cfg), None, 0, C.byref(count)))
+    out = (C.c_int32 * (8 * max(count.value, 1)))()
+    _check(lib, lib.waves_mg_plan(C.byref(cfg), out, count.value, C.byref(count)))
+    return [{"n": tuple(out[8 * l:8 * l + 3]), "f": tuple(out[8 * l + 3:8 * l + 6]), "stencil": out[8 * l + 6],
+             "aggregate": bool(out[8 * l + 7])} for l in range(count.value)]
+
+
 class WavesSolver:
     """One simulation on one CUDA device (a waves_handle)."""
 

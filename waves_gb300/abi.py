@@ -214,6 +214,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_config_beach",
     "waves_config_tank",
     "waves_dispersion_k",
+    "waves_mg_plan",
     "waves_create",
     "waves_destroy",
     "waves_request_steps",
@@ -260,6 +261,7 @@ def declare(lib):
         "waves_config_beach": (None, [cfgp]),
         "waves_config_tank": (None, [cfgp]),
         "waves_dispersion_k": (C.c_double, [C.c_double, C.c_double]),
+        "waves_mg_plan": (C.c_int, [P(WavesConfig), P(C.c_int32), C.c_int32, P(C.c_int32)]),
         "waves_create": (C.c_int, [cfgp, P(C.c_void_p)]),
         "waves_destroy": (None, [h]),
         "waves_request_steps": (C.c_int, [h, C.c_int64]),

@@ -162,12 +162,11 @@ std::vector<int> coarse_stencil(const std::vector<int>& st, const int f[3], bool
       }
   return result;
 }
-void plan_levels(waves_handle* h) {
-  const waves_config& k = h->cfg;
+void plan_levels_of(const waves_config& k, std::vector<HLevel>& levels) {
   int n[3] = {k.n[0], k.n[1], k.n[2]};
   double hh[3] = {double(k.spacing[0]), double(k.spacing[1]), double(k.spacing[2])};
   std::vector<int> st = {0, 0, 0, -1, 0, 0, 1, 0, 0, 0, -1, 0, 0, 1, 0, 0, 0, -1, 0, 0, 1};
-  h->levels.clear();
+  levels.clear();
   while (true) {
     int count = n[0] * n[1] * n[2];
     int f[3] = {1, 1, 1};
@@ -184,9 +183,9 @@ void plan_levels(waves_handle* h) {
     std::memcpy(lv.n, n, sizeof(n));
     lv.count = count;
     std::memcpy(lv.f, f, sizeof(f));
-    lv.aggregate = int(h->levels.size()) >= k.mg_aggregate_from;
+    lv.aggregate = int(levels.size()) >= k.mg_aggregate_from;
     lv.stencil = st;
-    h->levels.push_back(lv);
+    levels.push_back(lv);
     if (count <= 64 || (f[0] == 1 && f[1] == 1 && f[2] == 1)) break;
     st = coarse_stencil(st, f, lv.aggregate);
     for (int a = 0; a < 3; a++) {
@@ -195,6 +194,7 @@ void plan_levels(waves_handle* h) {
     }
   }
 }
+void plan_levels(waves_handle* h) { plan_levels_of(h->cfg, h->levels); }
 
 // solid() of pressure_core.glslinc:87-96 over (x, y) with a margin (z-independent geometry).
 bool solid_host(const waves_config& k, int x, int y) {
@@ -851,6 +851,26 @@ bool quota_met(const double* c, double quota) { return quota >= 0 ? c[2] >= quot
 
 // ====================================================================== C ABI
 extern "C" {
+
+waves_status waves_mg_plan(const waves_config* cfg, int32_t* out, int32_t capacity, int32_t* levels) {
+  if (!cfg || !levels || capacity < 0 || (capacity > 0 && !out)) return WAVES_INVALID_ARG;
+  if (cfg->n[0] < 1 || cfg->n[1] < 1 || cfg->n[2] < 1 || !(cfg->spacing[0] > 0.f) || !(cfg->spacing[1] > 0.f) ||
+      !(cfg->spacing[2] > 0.f))
+    return WAVES_INVALID_ARG;
+  std::vector<HLevel> plan;
+  plan_levels_of(*cfg, plan);
+  *levels = (int32_t)plan.size();
+  for (int l = 0; l < (int)plan.size() && l < capacity; l++) {
+    int32_t* o = out + 8 * l;
+    for (int a = 0; a < 3; a++) {
+      o[a] = plan[l].n[a];
+      o[3 + a] = plan[l].f[a];
+    }
+    o[6] = (int32_t)(plan[l].stencil.size() / 3);
+    o[7] = plan[l].aggregate ? 1 : 0;
+  }
+  return WAVES_OK;
+}
 
 waves_status waves_create(const waves_config* cfg, waves_handle** out) {
   if (!out || !cfg) return WAVES_INVALID_ARG;
