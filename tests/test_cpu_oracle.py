@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import waves_gb300 as wg
+from tests.cases import CASES
 from tests.oracle_ref import Oracle, lib
 
 
@@ -79,6 +80,19 @@ def test_beach_level_plan():
     sts = [s for _, s in levels]
     assert dims == [(310, 48, 80), (155, 24, 80), (78, 12, 40), (39, 6, 20), (20, 3, 10), (10, 2, 5), (5, 2, 5)]
     assert sts == [7, 39, 125, 27, 27, 27, 27]
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_product_level_plan_matches_the_oracle(name):
+    """The library's level plan (waves_mg_plan, the host function waves_create uses) against the
+    oracle's (pressure_multigrid.gd:37-69, :181-198) for every parity configuration: level sizes
+    and Galerkin stencil sizes (periodic x, odd extents, aggregation from level 2 or 3)."""
+    cfg = CASES[name]()
+    plan = wg.mg_plan(cfg)
+    assert [(l["n"], l["stencil"]) for l in plan] == Oracle(cfg, 32).levels()
+    for a, b in zip(plan, plan[1:]):
+        assert b["n"] == tuple((n + f - 1) // f for n, f in zip(a["n"], a["f"]))
+    assert [l["aggregate"] for l in plan] == [l >= cfg.mg_aggregate_from for l in range(len(plan))]
 
 
 def flat_tank(**kw):
