@@ -211,3 +211,52 @@ def test_render_oracle_known_answers():
     assert np.allclose(tr[hit, 2], 2.0, atol=2e-6)  # one interval, leaving through the floor
     # deeper water is darker in red (absorption 1.4 / 0.18 per metre) than the sky behind a miss
     assert np.all(img[hit, 0] < img[~hit, 0].min())
+
+
+def test_fixture5_velocity_is_the_discrete_curl_of_the_stokes_streamfunction():
+    """Op 40, fixture 5 (coupled_motion.glslinc:203-207,258-266; the surface eta of
+    pressure_core.glslinc:52-58): the initial x and y face velocities are centred differences of the
+    second-order Stokes streamfunction across each face, on faces up to three cells above the wave
+    surface that are not walls, and zero elsewhere; the initial commands that follow
+    (coupled_gpu.gd:34-37) do not touch velocities.  Evaluated independently here in FP64, against
+    the FP64 oracle; and since each velocity is a difference of one vertex streamfunction, every
+    cell with all four x/y faces set has zero discrete divergence."""
+    from tests.cases import wave_periodic
+    cfg = wave_periodic()
+    nx, ny, nz = cfg.n
+    hx, hy, _ = (float(v) for v in cfg.spacing)
+    ox, oy, _ = (float(v) for v in cfg.origin)
+    a, k, w, d = (float(v) for v in cfg.wave)
+    eta0 = float(cfg.eta)
+    N = nx * ny * nz
+    nu = (nx + 1) * ny * nz
+    bank = Oracle(cfg, 64).bank_d()
+    u = bank[N:N + nu].reshape(nz, ny, nx + 1)
+    v = bank[N + nu:N + nu + nx * (ny + 1) * nz].reshape(nz, ny + 1, nx)
+
+    def psi(x, y):
+        s = a * w / (k * math.sinh(k * d)) * np.sinh(k * (y + d)) * np.cos(k * x)
+        return s + 0.375 * a * a * w / math.sinh(k * d) ** 4 * np.sinh(2 * k * (y + d)) * np.cos(2 * k * x)
+
+    sigma = math.tanh(k * d)
+    second = k * a * a * (3 - sigma * sigma) / (4 * sigma ** 3)
+    eta = lambda qx: eta0 + a * np.cos(k * (ox + (qx + 0.5) * hx)) + second * np.cos(2 * k * (ox + (qx + 0.5) * hx))
+    # x faces (periodic in x: no walls; the floor is below y = 0): position of face (qx, qy)
+    qx, qy = np.meshgrid(np.arange(nx + 1), np.arange(ny), indexing="xy")
+    fx, fy = ox + qx * hx, oy + (qy + 0.5) * hy
+    band_u = fy < eta(qx) + 3 * hy
+    want_u = np.where(band_u, (psi(fx, fy + 0.5 * hy) - psi(fx, fy - 0.5 * hy)) / hy, 0.0)
+    # y faces: the bottom row (qy = 0) is a wall face
+    qx, qy = np.meshgrid(np.arange(nx), np.arange(ny + 1), indexing="xy")
+    fx, fy = ox + (qx + 0.5) * hx, oy + qy * hy
+    band_v = (fy < eta(qx) + 3 * hy) & (qy > 0)
+    want_v = np.where(band_v, -(psi(fx + 0.5 * hx, fy) - psi(fx - 0.5 * hx, fy)) / hx, 0.0)
+    scale = max(np.abs(want_u).max(), np.abs(want_v).max())
+    assert scale > 1e-3 and band_u.sum() > nx * 4
+    for z in range(nz):
+        assert np.abs(u[z] - want_u).max() <= 1e-9 * scale
+        assert np.abs(v[z] - want_v).max() <= 1e-9 * scale
+    assert np.abs(bank[N + nu + nx * (ny + 1) * nz:N + nu + nx * (ny + 1) * nz + nx * ny * (nz + 1)]).max() == 0.0
+    full = band_u[:, :-1] & band_u[:, 1:] & band_v[:-1, :] & band_v[1:, :]
+    div = (u[:, :, 1:] - u[:, :, :-1]) / hx + (v[:, 1:, :] - v[:, :-1, :]) / hy
+    assert full.sum() > nx and np.abs(div[:, full]).max() <= 1e-9 * scale / hx
