@@ -315,12 +315,11 @@ def step_roofline(plan, iters_per_step, builds_per_step, bf16, ms_per_step):
             "non_cg_bytes": model["non_cg"], "formula": STEP_BYTES_FORMULA}
 
 
-def cpu_baseline(args, cfg_mg, seconds):
-    """The oracle (CPU restatement, FP32, all host threads) on the beach for a bounded sample."""
-    from tests.oracle_ref import Oracle
-    cfg = beach_config(cfg_mg)
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+def oracle_sample(cfg, seconds, threads):
+    """Accepted steps of the oracle (FP32) from rest until `seconds` of wall time have passed, on
+    `threads` OpenMP threads (0: every processor): (sim-s per wall-s, threads, steps, sim-s, wall-s)."""
+    from tests.oracle_ref import Oracle, lib
+    used = lib().wo_set_threads(threads)
     o = Oracle(cfg, 32)
     t0 = time.perf_counter()
     steps = 0
@@ -329,9 +328,26 @@ def cpu_baseline(args, cfg_mg, seconds):
         o.request_steps(steps)
         o.run()
     wall = time.perf_counter() - t0
-    c = o.control()
-    return {"value": c[1] / wall, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)),
-            "kind": "port", "sample": f"{steps} accepted steps of the 310x48x80 beach from rest ({c[1]:.4f} sim-s, {wall:.1f} s)"}
+    sim = float(o.control()[1])
+    return sim / wall, used, steps, sim, wall
+
+
+def cpu_baseline(args, cfg_mg, seconds, single_core_seconds=0.0):
+    """The oracle (CPU restatement, FP32) on the beach for a bounded sample on every host core, and
+    optionally a second sample on one core."""
+    from tests.oracle_ref import lib
+    cfg = beach_config(cfg_mg)
+    try:
+        value, cores, steps, sim, wall = oracle_sample(cfg, seconds, 0)
+        out = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{steps} accepted steps of the 310x48x80 beach from rest ({sim:.4f} sim-s, {wall:.1f} s)"}
+        if single_core_seconds > 0:
+            v1, _, s1, sim1, w1 = oracle_sample(cfg, single_core_seconds, 1)
+            out["single_core"] = {"value": v1, "unit": UNIT, "cores": 1,
+                                  "sample": f"{s1} accepted steps from rest ({sim1:.4f} sim-s, {w1:.1f} s)"}
+    finally:
+        lib().wo_set_threads(0)
+    return out
 
 
 def main():
@@ -412,7 +428,7 @@ def main():
                        "frames": e["frames"], "window": "the timed steps' simulated span, from their starting state"}
     if world == 1 and not args.no_cpu_baseline:
         try:
-            base = cpu_baseline(args, args.mg, args.cpu_seconds)
+            base = cpu_baseline(args, args.mg, args.cpu_seconds, args.cpu_seconds / 2)
             line["cpu_baseline"] = base
         except Exception as ex:  # the oracle needs a C++ toolchain on the host
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(ex)[:200]}

@@ -6,6 +6,8 @@
 #include <memory>
 #include <string>
 
+#include <omp.h>
+
 #include "wo_solver.hpp"
 
 namespace {
@@ -28,6 +30,14 @@ template <class R> void copy_in(std::vector<R>& v, const float* in) {
 }  // namespace
 
 extern "C" {
+
+// OpenMP threads of the oracle's parallel loops (n <= 0: the number of processors); returns the
+// count in effect.  Every parallel loop writes disjoint outputs and every floating-point sum is
+// sequential, so results do not depend on it.
+int wo_set_threads(int n) {
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+  return omp_get_max_threads();
+}
 
 // precision 32: FP32 decision-parity oracle; 64: FP64 error oracle.  Runs the initial commands.
 void* wo_create(const waves_config* cfg, int precision) {

@@ -60,6 +60,7 @@ def lib():
             "wo_cube_volume_d": (C.c_double, [C.c_double] * 4),
             "wo_inverse_volume_d": (C.c_double, [C.c_double] * 4),
             "wo_time_batches": (C.c_double, [vp, C.c_int]),
+            "wo_set_threads": (C.c_int, [C.c_int]),
             "wo_phase": (None, [vp, C.c_int]),
             "wo_read": (C.c_int, [vp, C.c_char_p, fp]),
         }

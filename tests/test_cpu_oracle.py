@@ -121,14 +121,20 @@ def test_volume_conservation_ledger():
 
 
 def test_oracle_is_deterministic_and_thread_count_invariant():
+    """The same run twice on all threads and once on one thread: identical banks and control
+    block (the parallel loops write disjoint outputs; every floating-point sum is sequential)."""
     cfg = wg.config("beach", n=(64, 40, 8), origin=(0.5, -0.6, -0.2))
     runs = []
-    for _ in range(2):
-        o = Oracle(cfg, 32)
-        o.request_steps(3)
-        o.run()
-        runs.append(np.concatenate([o.bank(0), o.bank(1)]))
-    assert np.array_equal(runs[0], runs[1])
+    try:
+        for threads in (0, 0, 1):
+            assert lib().wo_set_threads(threads) >= 1
+            o = Oracle(cfg, 32)
+            o.request_steps(3)
+            o.run()
+            runs.append(np.concatenate([o.bank(0), o.bank(1), o.control()]))
+    finally:
+        lib().wo_set_threads(0)
+    assert np.array_equal(runs[0], runs[1]) and np.array_equal(runs[0], runs[2])
 
 
 def test_injected_rejection_and_retry_paths():
