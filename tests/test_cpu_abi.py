@@ -78,3 +78,55 @@ def test_render_defaults_without_gpu():
     tank = waves_gb300.config("tank")  # 16 x 0.05 m = 0.8 m deep in z: the close view
     lib.waves_render_params_default(C.byref(p), C.byref(tank), 64, 64)
     assert max(abs(a - b) for a, b in zip(p.target, (3.45, -0.08, 0.0))) < 1e-6 and abs(p.size - 1.5) < 1e-6
+
+
+def test_training_calls_check_their_arguments_and_need_a_device():
+    """waves_net_gradients / waves_net_train validate the batch before any CUDA call (bad sizes,
+    missing buffers, an unknown arithmetic, a tensor-core grid beyond 65,535 crop planes:
+    WAVES_INVALID_ARG), and without a GPU a valid batch is WAVES_NO_DEVICE, never a CPU fallback."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from waves_gb300.abi import WAVES_NET_EXACT, WAVES_NET_TENSOR, WavesNetBatch
+    from waves_gb300.learned import CHANNELS
+    lib = waves_gb300.load(build_if_missing=True)
+    fp = C.POINTER(C.c_float)
+    x = np.zeros((1, 3, 4, 4, 4), np.float32)
+    t = np.zeros((1, 4, 4, 4), np.float32)
+    ws = [np.zeros((co, 27, ci), np.float32) for ci, co in CHANNELS]
+    bs = [np.zeros(co, np.float32) for _, co in CHANNELS]
+    ptrs = lambda arrays: (fp * 4)(*[a.ctypes.data_as(fp) for a in arrays])
+    loss = C.c_double()
+
+    def grads(crops=1, nz=4, arithmetic=WAVES_NET_EXACT, mask=True):
+        bt = WavesNetBatch(crops, nz, 4, 4, x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+                           t.ctypes.data_as(fp) if mask else None, arithmetic)
+        return lib.waves_net_gradients(C.byref(bt), ptrs(ws), ptrs(bs), C.byref(loss), ptrs(ws), ptrs(bs), None, 0)
+
+    assert grads(crops=0) == 1 and grads(nz=0) == 1 and grads(mask=False) == 1
+    assert grads(arithmetic=2) == 1 and grads(arithmetic=-1) == 1
+    assert grads(crops=1000, nz=70, arithmetic=WAVES_NET_TENSOR) == 1  # 70,000 crop planes
+    bt = WavesNetBatch(1, 4, 4, 4, x.ctypes.data_as(fp), t.ctypes.data_as(fp), t.ctypes.data_as(fp), 0)
+    assert lib.waves_net_train(C.byref(bt), ptrs(ws), ptrs(bs), -1, 1e-3, None, 0) == 1
+    assert lib.waves_net_train(C.byref(bt), ptrs(ws), ptrs(bs), 1, 0.0, None, 0) == 1
+    if not torch.cuda.is_available():
+        assert grads() == 3 and grads(arithmetic=WAVES_NET_TENSOR) == 3
+        assert lib.waves_net_train(C.byref(bt), ptrs(ws), ptrs(bs), 1, 1e-3, None, 0) == 3
+
+
+def test_mg_plan_arguments():
+    """waves_mg_plan: the level count with no output buffer, only `capacity` levels written, and
+    WAVES_INVALID_ARG for a missing count, a negative capacity or an empty grid."""
+    import ctypes as C
+    lib = waves_gb300.load(build_if_missing=True)
+    cfg = waves_gb300.config("beach")
+    count = C.c_int32()
+    assert lib.waves_mg_plan(C.byref(cfg), None, 0, C.byref(count)) == 0 and count.value == 7
+    out = (C.c_int32 * 24)(*([-7] * 24))
+    assert lib.waves_mg_plan(C.byref(cfg), out, 2, C.byref(count)) == 0 and count.value == 7
+    assert list(out[:8]) == [310, 48, 80, 2, 2, 1, 7, 0] and list(out[16:]) == [-7] * 8
+    assert lib.waves_mg_plan(C.byref(cfg), out, 2, None) == 1
+    assert lib.waves_mg_plan(C.byref(cfg), out, -1, C.byref(count)) == 1
+    assert lib.waves_mg_plan(C.byref(cfg), None, 2, C.byref(count)) == 1
+    cfg.n[1] = 0
+    assert lib.waves_mg_plan(C.byref(cfg), out, 2, C.byref(count)) == 1
