@@ -88,3 +88,52 @@ def test_step_bytes_model_reproduces_the_algorithmic_byte_table():
     roof = bench.step_roofline(plan, 14.0, 0.5, False, 12.5)
     assert roof["achieved"] == pytest.approx(step["bytes_per_step"] / 12.5e-3 / 1e9)
     assert roof["frac"] == pytest.approx(roof["achieved"] / bench.measured_peaks()[0])
+
+
+def test_crop_bank_cuts_consistent_crops_and_scales_over_every_wet_cell():
+    """waves_gb300.learned.train.CropBank (crops cut while pairs are captured): every field of a
+    crop comes from the same offset of the same pair, the mask is the wet cells at least `edge`
+    inside, the scales are the population standard deviations over all wet cells of all pairs (as
+    if the pairs had been kept), and `rate` crops per pair are cut on average."""
+    import numpy as np
+    from waves_gb300.learned.train import CropBank
+    nx, ny, nz = 30, 12, 20
+    rng = np.random.default_rng(1)
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    pairs = []
+    for k in range(6):
+        wet = (y < 7 + k % 3) & (rng.random((nz, ny, nx)) < 0.9)
+        pairs.append({"F": (x + 100 * y + 10000 * z + 1e6 * k).astype(np.float32).ravel(),
+                      "b": rng.normal(3.0, 2.0, (nz, ny, nx)).astype(np.float32).ravel(),
+                      "p_prev": rng.normal(900.0, 300.0, (nz, ny, nx)).astype(np.float32).ravel(),
+                      "p_star": rng.normal(905.0, 301.0, (nz, ny, nx)).astype(np.float32).ravel(),
+                      "kind": np.where(wet, 1.0, 0.0).astype(np.float32).ravel()})
+    bank = CropBank((nx, ny, nz), 1.5, crop=(8, 8, 8), edge=2, seed=3)
+    for p in pairs:
+        bank.add(p)
+    assert 6 <= len(bank.raw) <= 12
+    xs, ys, ms, (s_b, s_p, s_out) = bank.batch()
+    wet_all = np.concatenate([p["kind"] > 0 for p in pairs])
+    cat = lambda key: np.concatenate([p[key] for p in pairs]).astype(np.float64)
+    dp = np.concatenate([p["p_star"] - p["p_prev"] for p in pairs]).astype(np.float64)
+    assert s_b == pytest.approx(1.0 / cat("b")[wet_all].std(), rel=1e-9)
+    assert s_p == pytest.approx(1.0 / cat("p_prev")[wet_all].std(), rel=1e-9)
+    assert s_out == pytest.approx(dp[wet_all].std(), rel=1e-9)
+    inner = np.zeros((8, 8, 8), bool)
+    inner[2:6, 2:6, 2:6] = True
+    for i in range(len(xs)):
+        code = int(xs[i, 0, 0, 0, 0])
+        k, oz, oy, ox = code // 1000000, (code // 10000) % 100, (code // 100) % 100, code % 100
+        assert 0 <= ox <= nx - 8 and 0 <= oy <= ny - 8 and 0 <= oz <= nz - 8
+        sl = (slice(oz, oz + 8), slice(oy, oy + 8), slice(ox, ox + 8))
+        g = lambda key: pairs[k][key].reshape(nz, ny, nx)[sl]
+        assert np.array_equal(xs[i, 0], g("F"))
+        assert np.array_equal(xs[i, 1], g("b") * np.float32(s_b))
+        assert np.array_equal(xs[i, 2], g("p_prev") * np.float32(s_p))
+        assert np.array_equal(ys[i], (g("p_star") - g("p_prev")) / np.float32(s_out))
+        assert np.array_equal(ms[i] > 0, (g("kind") > 0) & inner)
+    sparse = CropBank((nx, ny, nz), 0.25, crop=(8, 8, 8), seed=4)
+    for _ in range(10):
+        for p in pairs[:4]:
+            sparse.add(p)
+    assert sparse.pairs == 40 and 3 <= len(sparse.raw) <= 20

@@ -2,6 +2,11 @@
 
     python -m waves_gb300.learned.train --seeds 8 --pairs 40 --out model.npz [--eval-seeds 2] [--trainer torch]
 
+The 2000-pair learned configuration (seeds 1..20, 100 pairs each over t in [2, 10] s; held-out
+seeds 101..105; one 24^3 crop per pair, cut while capturing):
+
+    python -m waves_gb300.learned.train --seeds 20 --pairs 100 --t0 2 --gap 0.08 --crops 2000 --eval-seeds 5
+
 Capture: for each seed the 310x48x80 beach (the lab settings) runs with a wave amplitude drawn
 from U(0.04, 0.10) m and a period from U(1.2, 1.8) s (wavenumber by the same dispersion
 bisection as the presets, std::mt19937_64-independent: numpy's PCG64 seeded with the seed).  It
@@ -50,7 +55,7 @@ def beach(seed, warm=0):
     return cfg, amplitude, period
 
 
-def capture_trial(s, N, NF):
+def capture_trial(s, N, NF, with_coef=WITH_COEF):
     """One trial through the debug phases; the first round's (F, b, p_prev, p*, kind) or None."""
     s.debug_phase(0)
     c = s.control()
@@ -62,7 +67,7 @@ def capture_trial(s, N, NF):
     bank = s.bank(cand)
     F, p_prev = bank[:N].copy(), bank[N + NF:N + NF + N].copy()
     kind = s.geometry()[1].copy()
-    coef = s.debug_read("coef", 6 * N) if WITH_COEF else None
+    coef = s.debug_read("coef", 6 * N) if with_coef else None
     s.debug_phase(7)
     pair, rounds = None, 0
     while True:
@@ -84,8 +89,10 @@ def capture_trial(s, N, NF):
     return pair
 
 
-def capture(seeds, pairs, t0, gap):
-    out = []
+def capture(seeds, pairs, t0, gap, sink=None, with_coef=WITH_COEF):
+    """`pairs` solve pairs per seed at t0 + gap, t0 + 2 gap, ...: the list of pairs, or, with a
+    sink, each pair handed to sink(pair) as it is captured (none kept) and the count returned."""
+    out, count = [], 0
     for seed in seeds:
         cfg, a, T = beach(seed)
         s = wg.WavesSolver(cfg)
@@ -96,12 +103,77 @@ def capture(seeds, pairs, t0, gap):
             s.request_time(t0 + (k + 1) * gap)
             s.run()
             s.request_steps(int(s.control()[2]) + 1)
-            p = capture_trial(s, N, NF)
+            p = capture_trial(s, N, NF, with_coef)
             if p is not None:
-                out.append(p)
+                count += 1
+                if sink is None:
+                    out.append(p)
+                else:
+                    sink(p)
         s.close()
-        print(f"seed {seed}: a {a:.3f} m, T {T:.3f} s, {len(out)} pairs so far", flush=True)
-    return out
+        print(f"seed {seed}: a {a:.3f} m, T {T:.3f} s, {count} pairs so far", flush=True)
+    return out if sink is None else count
+
+
+class CropBank:
+    """Training crops cut from solve pairs as they are captured, so that no full pair is kept
+    (a beach pair is 24 MB; 2000 of them would not fit in host memory).  Each pair gives
+    `rate` crops on average (floor(rate), plus one with probability frac(rate)) at uniform random
+    offsets: F, b, p_prev and p* - p_prev, and the loss mask (wet cells at least `edge` cells inside
+    the crop).  The input and output scales are the population standard deviations over every wet
+    cell of every pair, from running sums."""
+
+    def __init__(self, n, rate, crop=(24, 24, 24), edge=4, seed=0):
+        self.nx, self.ny, self.nz = n
+        self.cx, self.cy, self.cz = min(crop[0], self.nx), min(crop[1], self.ny), min(crop[2], self.nz)
+        self.rate = float(rate)
+        self.rng = np.random.default_rng(seed)
+        self.inner = np.zeros((self.cz, self.cy, self.cx), np.float32)
+        self.inner[edge:self.cz - edge, edge:self.cy - edge, edge:self.cx - edge] = 1.0
+        self.raw = []
+        self.sums = np.zeros((3, 3))  # rows b, p_prev, p* - p_prev: count, sum, sum of squares
+        self.pairs = 0
+
+    def add(self, p):
+        grid = lambda a: np.asarray(a, dtype=np.float32).reshape(self.nz, self.ny, self.nx)
+        wet = grid(p["kind"]) > 0
+        F, b, pp = grid(p["F"]), grid(p["b"]), grid(p["p_prev"])
+        dp = grid(p["p_star"]) - pp
+        for row, a in enumerate((b, pp, dp)):
+            v = a[wet].astype(np.float64)
+            self.sums[row] += (v.size, v.sum(), float(np.dot(v, v)))
+        whole = int(self.rate)
+        count = whole + (1 if self.rng.random() < self.rate - whole else 0)
+        for _ in range(count):
+            ox = int(self.rng.integers(self.nx - self.cx + 1))
+            oy = int(self.rng.integers(self.ny - self.cy + 1))
+            oz = int(self.rng.integers(self.nz - self.cz + 1))
+            sl = (slice(oz, oz + self.cz), slice(oy, oy + self.cy), slice(ox, ox + self.cx))
+            self.raw.append((F[sl].copy(), b[sl].copy(), pp[sl].copy(), dp[sl].copy(),
+                             (wet[sl] * self.inner).astype(np.float32)))
+        self.pairs += 1
+
+    def scales(self):
+        """(s_b, s_p, s_out): inputs are multiplied by s_b and s_p, the target divided by s_out."""
+        def std(row):
+            n, s1, s2 = self.sums[row]
+            return math.sqrt(max(s2 / max(n, 1.0) - (s1 / max(n, 1.0)) ** 2, 0.0))
+        return 1.0 / max(std(0), 1e-12), 1.0 / max(std(1), 1e-12), max(std(2), 1e-12)
+
+    def batch(self):
+        """(x [crops][3][z][y][x], target, mask, scales) with the scales applied."""
+        s_b, s_p, s_out = self.scales()
+        k = len(self.raw)
+        xs = np.zeros((k, 3, self.cz, self.cy, self.cx), np.float32)
+        ys = np.zeros((k, self.cz, self.cy, self.cx), np.float32)
+        ms = np.zeros((k, self.cz, self.cy, self.cx), np.float32)
+        for i, (F, b, pp, dp, m) in enumerate(self.raw):
+            xs[i, 0] = F
+            xs[i, 1] = b * s_b
+            xs[i, 2] = pp * s_p
+            ys[i] = dp / s_out
+            ms[i] = m
+        return xs, ys, ms, (s_b, s_p, s_out)
 
 
 def build_net(torch):
@@ -196,39 +268,14 @@ def train(pairs, n, steps, seed, device, objective="residual"):
     return weights, biases, (1.0, s_b, s_p), s_out, resid / max(total, 1e-30)
 
 
-def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e-3, tensor=True):
+def train_cuda(bank, steps, seed=0, lr=2e-3, tensor=True):
     """The MSE objective trained with the library's own kernels (waves_net_train: forward, backward
-    and Adam on the GPU): a fixed batch of random crops of the training pairs, the loss counted on
-    wet cells at least `edge` cells from the crop edge; full-batch Adam for `steps` steps.  tensor:
-    the tensor-core arithmetic (WAVES_NET_TENSOR), else the oracle's (WAVES_NET_EXACT)."""
+    and Adam on the GPU) on the crops of a CropBank, the loss counted where the bank's mask is set;
+    full-batch Adam for `steps` steps.  tensor: the tensor-core arithmetic (WAVES_NET_TENSOR), else
+    the oracle's (WAVES_NET_EXACT)."""
     from waves_gb300.learned import net_gradients, net_train
-    nx, ny, nz = n
     rng = np.random.default_rng(seed)
-    grid = lambda a: np.asarray(a, dtype=np.float32).reshape(nz, ny, nx)
-    wet = [grid(p["kind"]) > 0 for p in pairs]
-    allw = np.concatenate([w.ravel() for w in wet])
-    b_all = np.concatenate([grid(p["b"]).ravel() for p in pairs])[allw]
-    pp_all = np.concatenate([grid(p["p_prev"]).ravel() for p in pairs])[allw]
-    dp_all = np.concatenate([(grid(p["p_star"]) - grid(p["p_prev"])).ravel() for p in pairs])[allw]
-    s_b = 1.0 / max(float(b_all.std()), 1e-12)
-    s_p = 1.0 / max(float(pp_all.std()), 1e-12)
-    s_out = max(float(dp_all.std()), 1e-12)
-    cx, cy, cz = min(crop[0], nx), min(crop[1], ny), min(crop[2], nz)
-    xs = np.zeros((crops, 3, cz, cy, cx), np.float32)
-    ys = np.zeros((crops, cz, cy, cx), np.float32)
-    ms = np.zeros((crops, cz, cy, cx), np.float32)
-    inner = np.zeros((cz, cy, cx), np.float32)
-    inner[edge:cz - edge, edge:cy - edge, edge:cx - edge] = 1.0
-    for k in range(crops):
-        i = int(rng.integers(len(pairs)))
-        ox, oy, oz = int(rng.integers(nx - cx + 1)), int(rng.integers(ny - cy + 1)), int(rng.integers(nz - cz + 1))
-        sl = (slice(oz, oz + cz), slice(oy, oy + cy), slice(ox, ox + cx))
-        p = pairs[i]
-        xs[k, 0] = grid(p["F"])[sl]
-        xs[k, 1] = grid(p["b"])[sl] * s_b
-        xs[k, 2] = grid(p["p_prev"])[sl] * s_p
-        ys[k] = (grid(p["p_star"])[sl] - grid(p["p_prev"])[sl]) / s_out
-        ms[k] = wet[i][sl] * inner
+    xs, ys, ms, (s_b, s_p, s_out) = bank.batch()
     weights = [rng.normal(0.0, 1.0 / np.sqrt(27 * ci), size=(co, 27, ci)).astype(np.float32) * (0.1 if co == 1 else 1.0)
                for ci, co in CHANNELS]
     biases = [np.zeros(co, np.float32) for _, co in CHANNELS]
@@ -236,7 +283,7 @@ def train_cuda(pairs, n, steps, seed, crops=32, crop=(24, 24, 24), edge=4, lr=2e
     weights, biases, hist = net_train(xs, ys, ms, weights, biases, steps, lr, tensor=tensor)
     print(f"cuda trainer ({'tensor' if tensor else 'exact'}): masked MSE {hist[0]:.4e} -> {hist[-1]:.4e} in {steps} steps ({time.time() - t0:.1f} s)", flush=True)
     total = float((ms * ys * ys).sum() / max(ms.sum(), 1.0))
-    left, _, _, _ = net_gradients(xs, ys, ms, weights, biases)
+    left, _, _, _ = net_gradients(xs, ys, ms, weights, biases, tensor=tensor)
     bits = [bf16_bits(w) for w in weights]
     return bits, biases, (1.0, s_b, s_p), s_out, left / max(total, 1e-30)
 
@@ -283,24 +330,30 @@ def main():
     ap.add_argument("--objective", default="residual", choices=["residual", "mse"])
     ap.add_argument("--trainer", default="cuda", choices=["cuda", "torch"],
                     help="cuda: the library's own training kernels (MSE objective); torch: PyTorch")
-    ap.add_argument("--crops", type=int, default=32)
+    ap.add_argument("--crops", type=int, default=32,
+                    help="--trainer cuda: training crops of 24^3 in all (cut from the pairs as they are captured)")
     ap.add_argument("--arithmetic", default="tensor", choices=["tensor", "exact"],
                     help="--trainer cuda: tensor-core implicit GEMM (tensor) or the oracle's order (exact)")
     args = ap.parse_args()
     cfg, _, _ = beach(1)
-    pairs = capture(range(1, args.seeds + 1), args.pairs, args.t0, args.gap)
+    seeds = range(1, args.seeds + 1)
     if args.trainer == "cuda":
+        # crops cut as pairs are captured: the host keeps crops, never whole pairs
         args.objective = "mse"
-        weights, biases, iscale, oscale, unexplained = train_cuda(pairs, tuple(cfg.n), args.steps, 0, args.crops,
-                                                                          tensor=args.arithmetic == "tensor")
+        bank = CropBank(tuple(cfg.n), args.crops / max(args.seeds * args.pairs, 1))
+        npairs = capture(seeds, args.pairs, args.t0, args.gap, sink=bank.add, with_coef=False)
+        weights, biases, iscale, oscale, unexplained = train_cuda(bank, args.steps, 0,
+                                                                  tensor=args.arithmetic == "tensor")
     else:
         import torch
         device = "cuda" if torch.cuda.is_available() else "cpu"
+        pairs = capture(seeds, args.pairs, args.t0, args.gap)
+        npairs = len(pairs)
         weights, biases, iscale, oscale, unexplained = train(pairs, tuple(cfg.n), args.steps, 0, device, args.objective)
     np.savez(args.out, **{f"w{l}": w for l, w in enumerate(weights)}, **{f"b{l}": b for l, b in enumerate(biases)},
              input_scale=np.array(iscale, np.float32), output_scale=np.float32(oscale),
-             pairs=len(pairs), seeds=args.seeds, unexplained=unexplained)
-    print(json.dumps({"pairs": len(pairs), "trainer": args.trainer, "objective": args.objective, "fraction_left": unexplained, "input_scale": iscale,
+             pairs=npairs, seeds=args.seeds, unexplained=unexplained)
+    print(json.dumps({"pairs": npairs, "trainer": args.trainer, "objective": args.objective, "fraction_left": unexplained, "input_scale": iscale,
                       "output_scale": oscale, "out": args.out}), flush=True)
     if args.eval_seeds > 0:
         evaluate(args.out, range(101, 101 + args.eval_seeds), args.eval_steps)
