@@ -137,3 +137,40 @@ def test_crop_bank_cuts_consistent_crops_and_scales_over_every_wet_cell():
         for p in pairs[:4]:
             sparse.add(p)
     assert sparse.pairs == 40 and 3 <= len(sparse.raw) <= 20
+
+
+def test_bench_json_line_contract(monkeypatch, capsys):
+    """bench.py's single JSON line from a stubbed measurement (the GPU part replaced): the keys the
+    line must carry, value = simulated seconds / device seconds, ms_per_step from the device time,
+    the kernel and whole-step rooflines, e2e with its copied bytes, and the clock record."""
+    import json
+    import sys
+    bench = load_bench()
+    wg.load(build_if_missing=True)
+
+    def measured(args, world, rank, local):
+        return {"sim_s": 2.0, "device_s": 3.0, "wall_s": 3.1, "steps": 240, "trials": 245, "motion_ms": 500.0,
+                "pressure_ms": 2500.0, "iters": 3103.0, "defect_rounds": 1, "launches": 123456,
+                "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}, "t_end": 2.04, "mg_builds": 63,
+                "probes": [{"kernel": "k_mgl_rows", "launches": 100, "ms": 1.5, "bytes": 100 * 8e6},
+                           {"kernel": "all", "launches": 900, "ms": 11.0, "bytes": 0.0}],
+                "plan": wg.mg_plan(wg.config("beach")),
+                "e2e": {"sim_s": 2.0, "wall_s": 3.2, "frames": 120, "h2d": 8, "d2h": 23809032}, "render": None}
+
+    monkeypatch.setattr(bench, "run_ours", measured)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--no-cpu-baseline"])
+    bench.main()
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "roofline", "step_roofline", "e2e", "clocks",
+                "gpu_launches"):
+        assert key in d, key
+    assert d["value"] == pytest.approx(2.0 / 3.0) and d["ms_per_step"] == pytest.approx(3000.0 / 240)
+    assert d["n_gpus"] == 1 and d["higher_is_better"] is True and d["gpu_launches"] == 123456
+    assert "workload" in d["config"] and "model" not in d["config"]
+    assert d["roofline"]["kernel"] == "k_mgl_rows" and d["roofline"]["unit"] == "GB/s"
+    step = bench.step_bytes_model(wg.mg_plan(wg.config("beach")), 3103.0 / 240, 63 / 240, False)
+    assert d["step_roofline"]["bytes_per_step"] == pytest.approx(step["bytes_per_step"])
+    assert d["e2e"]["value"] == pytest.approx(2.0 / 3.2) and d["e2e"]["d2h_bytes_per_step"] == 23809032
