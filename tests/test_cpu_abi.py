@@ -130,3 +130,20 @@ def test_mg_plan_arguments():
     assert lib.waves_mg_plan(C.byref(cfg), None, 2, C.byref(count)) == 1
     cfg.n[1] = 0
     assert lib.waves_mg_plan(C.byref(cfg), out, 2, C.byref(count)) == 1
+
+
+def test_headers_compile_as_c99_and_cpp11(tmp_path):
+    """include/waves.h and include/waves_debug.h are plain C: a C99 host, a C++11 host and FFI
+    generators (cgo, JNI, ctypes) read them, so they compile warning-free under -pedantic."""
+    import shutil
+    import subprocess
+    import pytest
+    inc = os.path.join(ROOT, "include")
+    for compiler, std, ext in (("gcc", "c99", "c"), ("g++", "c++11", "cpp")):
+        if not shutil.which(compiler):
+            pytest.skip(f"{compiler} missing")
+        src = tmp_path / f"h.{ext}"
+        src.write_text('#include "waves.h"\n#include "waves_debug.h"\nint main(void) { return 0; }\n')
+        r = subprocess.run([compiler, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc,
+                            "-fsyntax-only", str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
