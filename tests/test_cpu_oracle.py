@@ -266,3 +266,41 @@ def test_fixture5_velocity_is_the_discrete_curl_of_the_stokes_streamfunction():
     full = band_u[:, :-1] & band_u[:, 1:] & band_v[:-1, :] & band_v[1:, :]
     div = (u[:, :, 1:] - u[:, :, :-1]) / hx + (v[:, 1:, :] - v[:, :-1, :]) / hy
     assert full.sum() > nx and np.abs(div[:, full]).max() <= 1e-9 * scale / hx
+
+
+def tank_with(poison):
+    """The 24x16x8 tank (dt 1/120, CFL 0.5 summed over axes) with both banks poisoned on the host."""
+    cfg = wg.config("tank", n=(24, 16, 8))
+    o = Oracle(cfg, 32)
+    b = o.bank(0)
+    poison(b, cfg)
+    o.set_bank(0, b)
+    o.set_bank(1, b.copy())
+    o.request_steps(1)
+    o.run()
+    return cfg, o.control()
+
+
+def test_cfl_substep_control_shrinks_dt_for_a_fast_face():
+    """CFL control (coupled_motion.glslinc:364, ops 43/1): one x face at 40 m/s in the liquid makes
+    the trial's dt at most CFL * hx / 40, and the step is accepted without a failure."""
+    def fast(b, cfg):
+        nx, ny, nz = cfg.n
+        b[nx * ny * nz + (4 * ny + 3) * (nx + 1) + 12] = 40.0
+    cfg, c = tank_with(fast)
+    assert c[7] == 0 and c[2] == 1 and c[3] == 0
+    assert 0.0 < c[20] <= cfg.cfl * cfg.spacing[0] / 40.0 * (1 + 1e-6)
+    assert c[20] > 0.5 * cfg.cfl * cfg.spacing[0] / 40.0
+
+
+@pytest.mark.parametrize("value", [float("nan"), -0.5])
+def test_retries_exhaust_and_halt_on_a_poisoned_fraction(value):
+    """A volume fraction outside [0, 1] (or NaN) fails the sweep bound (code 10,
+    coupled_motion.glslinc:407); the trial is retried at half dt twice (c29 = 2 retries, dt 1/120
+    -> 1/480), then the third rejection halts the solver with code 10 and no accepted step."""
+    def poison(b, cfg):
+        nx, ny, nz = cfg.n
+        b[(4 * ny + 3) * nx + 12] = value
+    cfg, c = tank_with(poison)
+    assert c[7] == 10 and c[33] == 10 and c[29] == 2 and c[3] == 3 and c[2] == 0
+    assert c[20] == pytest.approx(cfg.dt / 4, rel=1e-6)
