@@ -57,9 +57,12 @@ def test_harness_argument_and_device_errors():
     r = subprocess.run([HARNESS, "--bogus"], capture_output=True, text=True)
     assert r.returncode == 1 and "usage" in r.stderr
     import torch
+    r = subprocess.run([HARNESS, "--preset", "ocean"], capture_output=True, text=True)
+    assert r.returncode == 1 and "unknown preset" in r.stderr
     if not torch.cuda.is_available():
-        r = subprocess.run([HARNESS, "--preset", "tank", "--steps", "1"], capture_output=True, text=True)
-        assert r.returncode == 2 and "waves_create" in r.stderr
+        for preset in ("tank", "beach", "large"):
+            r = subprocess.run([HARNESS, "--preset", preset, "--steps", "1"], capture_output=True, text=True)
+            assert r.returncode == 2 and "waves_create" in r.stderr, preset
 
 
 def test_render_defaults_without_gpu():

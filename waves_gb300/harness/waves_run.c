@@ -1,7 +1,7 @@
 /*
  * waves_run: headless driver of the waves solver step through the C ABI only (include/waves.h).
  *
- *   waves_run [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16]
+ *   waves_run [--preset beach|large|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16]
  *             [--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]
  *
  * It plays the role of the reference's lab runner (water/lab_runner.gd:49-73): it requests
@@ -50,14 +50,19 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "--view") && v && (!strcmp(v, "water") || !strcmp(v, "clay"))) view = !strcmp(v, "water"), i++;
     else if (!strcmp(a, "--size") && v && sscanf(v, "%dx%d", &width, &height) == 2 && width > 0 && height > 0) i++;
     else {
-      fprintf(stderr, "usage: %s [--preset beach|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16] "
+      fprintf(stderr, "usage: %s [--preset beach|large|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16] "
                       "[--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]\n", argv[0]);
       return 1;
     }
   }
   waves_config cfg;
   if (!strcmp(preset, "beach")) waves_config_beach(&cfg);
-  else if (!strcmp(preset, "tank")) waves_config_tank(&cfg);
+  else if (!strcmp(preset, "large")) {
+    /* the beach at half the spacing: 620 x 96 x 160 cells, 8 multigrid levels */
+    waves_config_beach(&cfg);
+    cfg.n[0] = 620, cfg.n[1] = 96, cfg.n[2] = 160;
+    cfg.spacing[0] = 0.0125f, cfg.spacing[1] = 0.0125f, cfg.spacing[2] = 0.025f;
+  } else if (!strcmp(preset, "tank")) waves_config_tank(&cfg);
   else if (!strcmp(preset, "default")) waves_config_default(&cfg);
   else {
     fprintf(stderr, "unknown preset %s\n", preset);
