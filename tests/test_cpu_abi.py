@@ -150,3 +150,30 @@ def test_headers_compile_as_c99_and_cpp11(tmp_path):
         r = subprocess.run([compiler, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc,
                             "-fsyntax-only", str(src)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_harness_reads_the_raw_model_file(tmp_path):
+    """waves_run --model: the raw file of waves_gb300.learned.write_raw_model (31,324 bytes for the
+    3-16-16-16-1 network) is read and checked before any device call; a truncated file, trailing
+    bytes or a wrong tag exit 1, and a valid file gets as far as waves_create (exit 2 without a
+    GPU)."""
+    import subprocess
+    import torch
+    from waves_gb300.build import HARNESS, build
+    from waves_gb300.learned import write_raw_model
+    build()
+    good = tmp_path / "model.bin"
+    write_raw_model(os.path.join(ROOT, "waves_gb300", "learned", "model_beach.npz"), good)
+    data = good.read_bytes()
+    assert len(data) == 8 + sum(co * 27 * ci * 2 + co * 4 for ci, co in [(3, 16), (16, 16), (16, 16), (16, 1)]) + 16
+    bad = {"short": data[:-4], "long": data + b"\0", "tag": b"WVNET2\0\0" + data[8:]}
+    for name, content in bad.items():
+        path = tmp_path / f"{name}.bin"
+        path.write_bytes(content)
+        r = subprocess.run([HARNESS, "--preset", "tank", "--steps", "1", "--model", str(path)], capture_output=True,
+                           text=True)
+        assert r.returncode == 1 and "bad model file" in r.stderr, name
+    if not torch.cuda.is_available():
+        r = subprocess.run([HARNESS, "--preset", "beach", "--steps", "1", "--model", str(good)], capture_output=True,
+                           text=True)
+        assert r.returncode == 2 and "waves_create" in r.stderr

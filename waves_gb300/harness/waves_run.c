@@ -3,15 +3,20 @@
  *
  *   waves_run [--preset beach|large|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16]
  *             [--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]
+ *             [--model FILE]
  *
  * It plays the role of the reference's lab runner (water/lab_runner.gd:49-73): it requests
  * accepted time frame by frame (1/60 s by default, request_time), runs the solver until each
  * frame's quota is met, and prints one JSON line per run with the telemetry of waves_stats and
  * the device time of waves_timing.  --surface writes the last accepted surface export (float4
  * planes then float kinds, ops 19/14) to a file; --image renders the last accepted surface
- * (waves_render, the default camera of the configuration) to a binary PPM, sRGB-encoded.  The
- * exit status is 0 on success, 1 on a bad
- * argument, 2 when the library fails, 3 when the solver halts.
+ * (waves_render, the default camera of the configuration) to a binary PPM, sRGB-encoded.  --model
+ * loads a learned warm start (waves_set_warm_start, warm_start = 1) from the raw model file that
+ * waves_gb300.learned.write_raw_model writes: the 8 bytes "WVNET1\0\0", then per layer
+ * (3 -> 16 -> 16 -> 16 -> 1 channels) the BF16 weights [co][27][ci] as little-endian uint16 and
+ * the FP32 biases [co], then the three FP32 input scales and the FP32 output scale.  The exit
+ * status is 0 on success, 1 on a bad argument (or model file), 2 when the library fails, 3 when
+ * the solver halts.
  */
 #define _POSIX_C_SOURCE 199309L
 #include <math.h>
@@ -21,6 +26,30 @@
 #include <time.h>
 
 #include "waves.h"
+
+/* The learned warm start of a raw model file (format above): 0 on success, -1 on a bad file. */
+static const int kCi[WAVES_NET_LAYERS] = {3, 16, 16, 16}, kCo[WAVES_NET_LAYERS] = {16, 16, 16, 1};
+static uint16_t* g_weights[WAVES_NET_LAYERS];
+static float* g_bias[WAVES_NET_LAYERS];
+static int read_model(const char* path, waves_warm_start_model* m) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return -1;
+  char magic[8];
+  int ok = fread(magic, 1, 8, f) == 8 && !memcmp(magic, "WVNET1\0\0", 8);
+  for (int l = 0; ok && l < WAVES_NET_LAYERS; l++) {
+    const size_t nw = (size_t)kCo[l] * 27 * kCi[l];
+    g_weights[l] = (uint16_t*)malloc(nw * sizeof(uint16_t));
+    g_bias[l] = (float*)malloc((size_t)kCo[l] * sizeof(float));
+    ok = g_weights[l] && g_bias[l] && fread(g_weights[l], sizeof(uint16_t), nw, f) == nw &&
+         fread(g_bias[l], sizeof(float), (size_t)kCo[l], f) == (size_t)kCo[l];
+    m->weights[l] = g_weights[l];
+    m->bias[l] = g_bias[l];
+  }
+  ok = ok && fread(m->input_scale, sizeof(float), 3, f) == 3 && fread(&m->output_scale, sizeof(float), 1, f) == 1;
+  ok = ok && fgetc(f) == EOF;
+  fclose(f);
+  return ok ? 0 : -1;
+}
 
 static double now_s(void) {
   struct timespec t;
@@ -32,6 +61,7 @@ int main(int argc, char** argv) {
   const char* preset = "beach";
   const char* surface = NULL;
   const char* image = NULL;
+  const char* model_path = NULL;
   int view = 1, width = 1280, height = 720;
   double seconds = 1.0, frame = 1.0 / 60.0, tol = 1e-6;
   long steps = 0;
@@ -47,11 +77,13 @@ int main(int argc, char** argv) {
     else if (!strcmp(a, "--frame") && v) frame = atof(v), i++;
     else if (!strcmp(a, "--surface") && v) surface = v, i++;
     else if (!strcmp(a, "--image") && v) image = v, i++;
+    else if (!strcmp(a, "--model") && v) model_path = v, i++;
     else if (!strcmp(a, "--view") && v && (!strcmp(v, "water") || !strcmp(v, "clay"))) view = !strcmp(v, "water"), i++;
     else if (!strcmp(a, "--size") && v && sscanf(v, "%dx%d", &width, &height) == 2 && width > 0 && height > 0) i++;
     else {
       fprintf(stderr, "usage: %s [--preset beach|large|tank|default] [--seconds S | --steps K] [--tol T] [--mg 32|16] "
-                      "[--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH]\n", argv[0]);
+                      "[--frame DT] [--surface FILE] [--image FILE.ppm] [--view water|clay] [--size WxH] [--model FILE]\n",
+              argv[0]);
       return 1;
     }
   }
@@ -70,10 +102,24 @@ int main(int argc, char** argv) {
   }
   cfg.pressure_tolerance = (float)tol;
   cfg.mg_precision = mg;
+  waves_warm_start_model model;
+  memset(&model, 0, sizeof(model));
+  if (model_path) {
+    if (read_model(model_path, &model) != 0) {
+      fprintf(stderr, "bad model file %s\n", model_path);
+      return 1;
+    }
+    cfg.warm_start = 1;
+  }
   waves_handle* h = NULL;
   waves_status st = waves_create(&cfg, &h);
   if (st != WAVES_OK) {
     fprintf(stderr, "waves_create: %d %s\n", (int)st, waves_last_error(NULL));
+    return 2;
+  }
+  if (model_path && (st = waves_set_warm_start(h, &model)) != WAVES_OK) {
+    fprintf(stderr, "waves_set_warm_start: %d %s\n", (int)st, waves_last_error(h));
+    waves_destroy(h);
     return 2;
   }
   int halted = 0;

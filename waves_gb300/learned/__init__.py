@@ -26,6 +26,23 @@ def load_model(path):
     return weights, biases, tuple(float(v) for v in z["input_scale"]), float(z["output_scale"])
 
 
+def write_raw_model(npz_path, out_path):
+    """The model of a train.py file as the raw file waves_run --model reads: b"WVNET1\\0\\0", per
+    layer the BF16 weights [co][27][ci] (little-endian uint16) and the FP32 biases [co], then the
+    three FP32 input scales and the FP32 output scale."""
+    weights, biases, iscale, oscale = load_model(npz_path)
+    with open(out_path, "wb") as f:
+        f.write(b"WVNET1\0\0")
+        for w, b, (ci, co) in zip(weights, biases, CHANNELS):
+            w = np.asarray(w)
+            bits = w.astype("<u2") if w.dtype == np.uint16 else bf16_bits(w).astype("<u2")
+            assert bits.size == co * 27 * ci and np.asarray(b).size == co
+            f.write(np.ascontiguousarray(bits).tobytes())
+            f.write(np.asarray(b, dtype="<f4").tobytes())
+        f.write(np.asarray(iscale, dtype="<f4").tobytes())
+        f.write(np.asarray([oscale], dtype="<f4").tobytes())
+
+
 def _batch(x, target, mask, tensor):
     from waves_gb300.abi import WAVES_NET_EXACT, WAVES_NET_TENSOR, WavesNetBatch
     fp = C.POINTER(C.c_float)
