@@ -174,3 +174,52 @@ def test_bench_json_line_contract(monkeypatch, capsys):
     step = bench.step_bytes_model(wg.mg_plan(wg.config("beach")), 3103.0 / 240, 63 / 240, False)
     assert d["step_roofline"]["bytes_per_step"] == pytest.approx(step["bytes_per_step"])
     assert d["e2e"]["value"] == pytest.approx(2.0 / 3.2) and d["e2e"]["d2h_bytes_per_step"] == 23809032
+
+
+def test_gdscript_mirror_frame_packet_and_quota_without_a_gpu():
+    """waves_gb300.gd: request(steps) is a positive accepted-step quota and request_time(t) a
+    negative deadline (pressure_gpu.gd:48-54), forwarded before every frame; the frame's telemetry
+    packet carries the work_scheduler.gd:40,86 keys; frame() is False once idle or halted, and a
+    closed solver does nothing.  The solver is a fake standing in for the CUDA one."""
+    from waves_gb300.gd import CoastalGPU
+
+    class Fake:
+        def __init__(self):
+            self.calls = []
+            self.report = {"trials_submitted": 3, "queue_depth": 2, "predicted_gpu_ms": 1.5, "gpu_ms_total": 4.0,
+                           "r_fluid": 0.9, "accepted_steps": 7, "accepted_time": 0.05, "idle": 0, "halted": 0}
+
+        def request_steps(self, n):
+            self.calls.append(("steps", n))
+
+        def request_time(self, t):
+            self.calls.append(("time", t))
+
+        def frame(self, **budget):
+            self.calls.append(("frame", budget))
+            return dict(self.report)
+
+        def close(self):
+            self.calls.append(("close",))
+
+    packets = []
+    g = CoastalGPU({"n": (310, 48, 80)})
+    g.connect(packets.append)
+    g.solver = fake = Fake()
+    g.request_time(1.0)
+    assert g.frame() is True
+    assert fake.calls[0] == ("time", 1.0) and fake.calls[1][0] == "frame"
+    assert fake.calls[1][1] == {"gpu_budget_ms": 14.0, "max_inflight": 3, "max_trials": 96, "cpu_budget_ms": 4.0}
+    p = packets[-1]
+    assert p["submission_chunks"] == 3 and p["queue_depth"] == 2 and p["R_fluid"] == 0.9 and p["failure"] == 0
+    assert p["predicted_gpu_ns"] == pytest.approx(1.5e6) and p["gpu_ns"] == pytest.approx(4.0e6)
+    assert p["submission_accepted_steps"] == 7 and g.last_stats["accepted_time"] == 0.05
+    g.request(12)
+    fake.report["idle"] = 1
+    assert g.frame() is False and ("steps", 12) in fake.calls
+    fake.report.update(idle=0, halted=1)
+    assert g.frame() is False and packets[-1]["failure"] == 1
+    with pytest.raises(AssertionError):
+        g.request_time(float("nan"))
+    g.close()
+    assert ("close",) in fake.calls and g.frame() is False and g.solver is None
