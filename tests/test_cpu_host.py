@@ -223,3 +223,47 @@ def test_gdscript_mirror_frame_packet_and_quota_without_a_gpu():
         g.request_time(float("nan"))
     g.close()
     assert ("close",) in fake.calls and g.frame() is False and g.solver is None
+
+
+def test_train_cli_flow_with_fakes(tmp_path, monkeypatch):
+    """python -m waves_gb300.learned.train with the GPU parts replaced (capture feeds synthetic pairs
+    into the crop bank; net_train / net_gradients are fakes): the CUDA-trainer flow cuts the
+    requested number of crops on average, trains on them with the tensor arithmetic, and writes a
+    model file load_model reads back, with the pair count."""
+    import sys
+    import numpy as np
+    import waves_gb300.learned as learned
+    import waves_gb300.learned.train as train
+    nx, ny, nz = 310, 48, 80
+    seen = {}
+
+    def fake_capture(seeds, pairs, t0, gap, sink=None, with_coef=True):
+        assert sink is not None and with_coef is False
+        rng = np.random.default_rng(0)
+        count = 0
+        for _ in seeds:
+            for _ in range(pairs):
+                f = rng.random(nx * ny * nz).astype(np.float32)
+                sink({"F": f, "b": f - 0.5, "p_prev": 2 * f, "p_star": 2 * f + 0.1 * f * f, "kind": (f > 0.3).astype(np.float32)})
+                count += 1
+        return count
+
+    def fake_train(x, target, mask, weights, biases, iterations, lr, device=0, tensor=False):
+        seen.update(crops=x.shape[0], shape=x.shape[1:], tensor=tensor, iterations=iterations)
+        return weights, biases, np.linspace(1.0, 0.5, iterations)
+
+    def fake_gradients(x, target, mask, weights, biases, device=0, tensor=False):
+        return 0.25, None, None, None
+
+    monkeypatch.setattr(train, "capture", fake_capture)
+    monkeypatch.setattr(learned, "net_train", fake_train)
+    monkeypatch.setattr(learned, "net_gradients", fake_gradients)
+    out = tmp_path / "m.npz"
+    monkeypatch.setattr(sys, "argv", ["train", "--seeds", "2", "--pairs", "3", "--crops", "12", "--steps", "5",
+                                      "--eval-seeds", "0", "--out", str(out)])
+    train.main()
+    assert seen["tensor"] is True and seen["iterations"] == 5 and seen["shape"] == (3, 24, 24, 24)
+    assert 6 <= seen["crops"] <= 18  # 2 crops per pair on average
+    weights, biases, iscale, oscale = learned.load_model(str(out))
+    assert [w.shape for w in weights] == [(co, 27, ci) for ci, co in learned.CHANNELS] and weights[0].dtype == np.uint16
+    assert iscale[0] == 1.0 and oscale > 0 and int(np.load(out)["pairs"]) == 6
