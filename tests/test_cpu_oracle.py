@@ -304,3 +304,23 @@ def test_retries_exhaust_and_halt_on_a_poisoned_fraction(value):
     cfg, c = tank_with(poison)
     assert c[7] == 10 and c[33] == 10 and c[29] == 2 and c[3] == 3 and c[2] == 0
     assert c[20] == pytest.approx(cfg.dt / 4, rel=1e-6)
+
+
+def test_initial_surface_is_the_still_water_ramp_with_corrugation():
+    """Op 0 (pressure_pass.glslinc:14-17) with the corrugated surface of pressure_core.glslinc:61:
+    F = clamp(0.5 - (y_c - eta(x))/hy, 0, 1) with eta = eta0 + corrugation cos(2 pi (qx + 1/2)/nx)
+    (the shader's 6.28318530718), unchanged by the rest of the initial commands; and the initial
+    volume c26 is the sum of F times the cell volume.  Independent FP64 evaluation against the FP64
+    oracle."""
+    cfg = wg.config("default", n=(24, 24, 8), corrugation=0.03, corrugation_phase=0.0)
+    nx, ny, nz = cfg.n
+    hx, hy, hz = (float(v) for v in cfg.spacing)
+    o = Oracle(cfg, 64)
+    F = o.bank_d()[:nx * ny * nz].reshape(nz, ny, nx)
+    eta = float(cfg.eta) + float(cfg.corrugation) * np.cos(6.28318530718 * (np.arange(nx) + 0.5) / nx)
+    yc = float(cfg.origin[1]) + (np.arange(ny) + 0.5) * hy
+    want = np.clip(0.5 - (yc[:, None] - eta[None, :]) / hy, 0.0, 1.0)
+    assert 0.0 < want.mean() < 1.0 and np.unique(want).size > 10
+    for z in range(nz):
+        assert np.abs(F[z] - want).max() <= 1e-12
+    assert o.control()[26] == pytest.approx(F.sum() * hx * hy * hz, rel=1e-12)
