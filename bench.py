@@ -334,9 +334,10 @@ def oracle_sample(cfg, seconds, threads):
 
 def cpu_baseline(args, cfg_mg, seconds, single_core_seconds=0.0):
     """The oracle (CPU restatement, FP32) on the beach for a bounded sample on every host core, and
-    optionally a second sample on one core."""
-    from tests.oracle_ref import lib
-    cfg = beach_config(cfg_mg)
+    optionally a second sample on one core.  The configuration comes from the oracle's own presets
+    (oracle/wo_config.cpp): this leg loads nothing of the product library."""
+    from tests.oracle_ref import lib, oracle_config
+    cfg = oracle_config("beach", pressure_tolerance=TOL, mg_precision=cfg_mg)
     try:
         value, cores, steps, sim, wall = oracle_sample(cfg, seconds, 0)
         out = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",

@@ -343,9 +343,11 @@ waves_status waves_net_train(const waves_net_batch* batch, float* const* weights
  * for hosts that cannot let the library call cudaMalloc (engine-owned GPU memory, no allocation
  * inside a frame); its scratch is a fixed 64 KiB device array in the library, so it accepts at most
  * 2,097,152 cells (WAVES_INVALID_ARG beyond).  The first call on a device resolves that array's
- * address for the current device; make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race.  Bit-identical to waves_stats().initial_volume_m3 for the
- * solver's initial F. */
+ * address in the current CUDA context and keeps it, keyed by device and context id (so it is
+ * resolved again after cudaDeviceReset or in another context); make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU race.  The additions
+ * follow the solver's own volume reduction in the same order, so the result is bit-identical to
+ * waves_stats().initial_volume_m3 for the solver's initial F. */
 waves_status waves_liquid_volume_noalloc(const float* F, int32_t nx, int32_t ny, int32_t nz, float hx, float hy, float hz,
                                          double* out, void* stream);
 

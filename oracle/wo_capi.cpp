@@ -86,6 +86,11 @@ void wo_set_bank(void* h, int bank, const float* in) {
 void wo_get_geometry(void* h, float* phi, float* kind) {
   with(h, [&](auto& s) { copy_out(s.gphi, phi); copy_out(s.gkind, kind); return 0; });
 }
+// Signed distance and kind of every cell (the geometry a trial leaves for the next one), e.g. from a
+// state the GPU reached.
+void wo_set_geometry(void* h, const float* phi, const float* kind) {
+  with(h, [&](auto& s) { copy_in(s.gphi, phi); copy_in(s.gkind, kind); return 0; });
+}
 // Pressure masks and valid bands of both banks: pmask[2N], vband[2 faces].
 void wo_get_masks(void* h, float* pmask, float* vband) {
   with(h, [&](auto& s) {

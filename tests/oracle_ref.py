@@ -45,6 +45,7 @@ def lib():
             "wo_get_geometry": (None, [vp, fp, fp]),
             "wo_get_masks": (None, [vp, fp, fp]),
             "wo_set_masks": (None, [vp, fp, fp]),
+            "wo_set_geometry": (None, [vp, fp, fp]),
             "wo_get_export": (None, [vp, fp, fp]),
             "wo_render": (None, [fp, fp, C.POINTER(WavesConfig), C.POINTER(WavesRenderParams), C.c_float, fp, fp]),
             "wo_get_probes": (None, [vp, fp]),
@@ -63,6 +64,10 @@ def lib():
             "wo_set_threads": (C.c_int, [C.c_int]),
             "wo_phase": (None, [vp, C.c_int]),
             "wo_read": (C.c_int, [vp, C.c_char_p, fp]),
+            "wo_dispersion_k": (C.c_double, [C.c_double, C.c_double]),
+            "wo_config_default": (None, [C.POINTER(WavesConfig)]),
+            "wo_config_beach": (None, [C.POINTER(WavesConfig)]),
+            "wo_config_tank": (None, [C.POINTER(WavesConfig)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -70,6 +75,22 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def oracle_config(preset="default", **overrides):
+    """A WavesConfig from the oracle's own presets (oracle/wo_config.cpp: 'default', 'beach',
+    'tank'), with field overrides; the product library is not loaded."""
+    L = lib()
+    cfg = WavesConfig()
+    {"default": L.wo_config_default, "beach": L.wo_config_beach, "tank": L.wo_config_tank}[preset](C.byref(cfg))
+    for k, v in overrides.items():
+        field = getattr(cfg, k)
+        if hasattr(field, "__len__"):
+            for i, x in enumerate(v):
+                field[i] = x
+        else:
+            setattr(cfg, k, v)
+    return cfg
 
 
 def _fp(a):
@@ -136,6 +157,10 @@ class Oracle:
         kind = np.empty(self.N, dtype=np.float32)
         self.L.wo_get_geometry(self.h, _fp(phi), _fp(kind))
         return phi, kind
+
+    def set_geometry(self, phi, kind):
+        self.L.wo_set_geometry(self.h, _fp(np.ascontiguousarray(phi, dtype=np.float32)),
+                               _fp(np.ascontiguousarray(kind, dtype=np.float32)))
 
     def masks(self):
         pm = np.empty(2 * self.N, dtype=np.float32)

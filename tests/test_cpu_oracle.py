@@ -324,3 +324,15 @@ def test_initial_surface_is_the_still_water_ramp_with_corrugation():
     for z in range(nz):
         assert np.abs(F[z] - want).max() <= 1e-12
     assert o.control()[26] == pytest.approx(F.sum() * hx * hy * hz, rel=1e-12)
+
+
+@pytest.mark.parametrize("preset", ["default", "beach", "tank"])
+def test_oracle_presets_equal_the_product_presets(preset):
+    """The oracle builds its configurations itself (oracle/wo_config.cpp, restating
+    lab_runner.gd:19-26 and the GDScript defaults), so the CPU baseline never loads the product
+    library; both sets of presets fill the struct with the same bits."""
+    import ctypes as C
+    from tests.oracle_ref import oracle_config
+    mine, product = oracle_config(preset), wg.config(preset)
+    assert C.string_at(C.addressof(mine), C.sizeof(mine)) == C.string_at(C.addressof(product), C.sizeof(product))
+    assert lib().wo_dispersion_k(1.4, 0.45) == wg.dispersion_k(1.4, 0.45)

@@ -60,3 +60,16 @@ def test_adam_fits_a_teacher_network(gpu_lib, tensor):
     loss_after, _, _, _ = net_gradients(x, target, m, w, b)
     assert loss_after <= hist[-1] * 1.5
     assert all(wl.shape == (co, 27, ci) for wl, (ci, co) in zip(w, CHANNELS))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tensor", [False, True])
+def test_training_is_bitwise_reproducible(gpu_lib, tensor):
+    """Every sum of a training step (loss, weight and bias gradients) is reduced in a fixed order,
+    so two runs of the same Adam steps give the same loss history and weights bit for bit."""
+    x, t, m, weights, biases = random_batch(8, B=2, n=(10, 8, 12))
+    runs = [net_train(x, t, m, weights, biases, 5, 3e-3, tensor=tensor) for _ in range(2)]
+    (w0, b0, h0), (w1, b1, h1) = runs
+    assert np.array_equal(h0, h1)
+    for l in range(4):
+        assert np.array_equal(w0[l], w1[l]) and np.array_equal(b0[l], b1[l]), l

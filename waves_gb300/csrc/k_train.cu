@@ -61,10 +61,11 @@ __global__ void __launch_bounds__(NTT) k_tr_forward(const Crop S, int ci_n, int 
   if (a_next) a_next[idx] = bf16r(acc > 0.f ? acc : 0.f);
 }
 
-// dL/dy = 2 mask (y - target) / norm per cell; the loss sum in FP64 (one atomic per block).
+// dL/dy = 2 mask (y - target) / norm per cell; the loss in FP64: each block writes its partial sum,
+// k_tr_loss_sum adds the partials in a fixed order, so the loss is the same bits on every run.
 __global__ void __launch_bounds__(NTT) k_tr_loss(long long n, const float* __restrict__ y, const float* __restrict__ t,
                                                 const float* __restrict__ m, double norm, float* __restrict__ g,
-                                                double* loss) {
+                                                double* __restrict__ loss_part) {
   __shared__ double part[NTT];
   const long long i = (long long)blockIdx.x * NTT + threadIdx.x;
   double l = 0.0;
@@ -79,7 +80,22 @@ __global__ void __launch_bounds__(NTT) k_tr_loss(long long n, const float* __res
     if (threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(loss, part[0] / norm);
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = part[0];
+}
+
+// One block: thread j adds partials j, j + NTT, ... in turn, then a fixed tree; loss = sum / norm.
+__global__ void __launch_bounds__(NTT) k_tr_loss_sum(long long nparts, const double* __restrict__ loss_part,
+                                                    double norm, double* __restrict__ loss) {
+  __shared__ double part[NTT];
+  double s = 0.0;
+  for (long long b = threadIdx.x; b < nparts; b += NTT) s += loss_part[b];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = NTT / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) part[threadIdx.x] += part[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *loss = part[0] / norm;
 }
 
 // dL/dW[co][t][ci] = sum_b sum_cell g[b][co][cell] a[b][ci][cell + off_t]: one block per weight;
@@ -430,6 +446,7 @@ struct Trainer {
   float *mw[kLayers] = {}, *vw[kLayers] = {}, *mb[kLayers] = {}, *vb[kLayers] = {};
   float *a[kLayers] = {}, *z[kLayers] = {};
   double* loss = nullptr;
+  double* loss_part = nullptr;  // per-block partial sums of the loss
   cudaError_t err = cudaSuccess;
   // WAVES_NET_TENSOR operands: BF16 activations and gradients, B fragments, weight-gradient partials
   bool tc = false;
@@ -464,6 +481,7 @@ struct Trainer {
     g = alloc<float>(16 * cells);
     ga = alloc<float>(16 * cells);
     loss = alloc<double>(1);
+    loss_part = alloc<double>(blocks((long long)cells));
     if (tc) {
       const unsigned bx = (unsigned)((S.nx + TX - 1) / TX), by = (unsigned)((S.ny + TY - 1) / TY);
       const unsigned chunks = (unsigned)((S.nz + kZChunk - 1) / kZChunk);
@@ -519,8 +537,8 @@ struct Trainer {
     for (int l = 0; l < kLayers; l++)
       k_tr_forward<<<blocks(cells * kOut[l]), NTT>>>(S, kIn[l], kOut[l], a[l], wb[l], b[l], z[l],
                                                       l + 1 < kLayers ? a[l + 1] : nullptr);
-    cudaMemsetAsync(loss, 0, sizeof(double));
-    k_tr_loss<<<blocks(cells), NTT>>>(cells, z[kLayers - 1], t, m, norm, g, loss);
+    k_tr_loss<<<blocks(cells), NTT>>>(cells, z[kLayers - 1], t, m, norm, g, loss_part);
+    k_tr_loss_sum<<<1, NTT>>>((long long)blocks(cells), loss_part, norm, loss);
     for (int l = kLayers - 1; l >= 0; l--) {
       k_tr_grad_w<<<(unsigned)(nw(l) + kOut[l]), NTT>>>(S, kIn[l], kOut[l], g, a[l], gw[l], gb[l]);
       if (l == 0) break;
@@ -538,8 +556,8 @@ struct Trainer {
       k_tc_conv<2, 0><<<conv_grid, NTT>>>(S, act16[l], fw[l], b[l], kOut[l], nullptr, z[l], act16[l + 1]);
     k_tc_conv<1, 1><<<conv_grid, NTT>>>(S, act16[kLayers - 1], fw[kLayers - 1], b[kLayers - 1], kOut[kLayers - 1],
                                         nullptr, z[kLayers - 1], nullptr);
-    cudaMemsetAsync(loss, 0, sizeof(double));
-    k_tr_loss<<<blocks(cells), NTT>>>(cells, z[kLayers - 1], t, m, norm, g, loss);
+    k_tr_loss<<<blocks(cells), NTT>>>(cells, z[kLayers - 1], t, m, norm, g, loss_part);
+    k_tr_loss_sum<<<1, NTT>>>((long long)blocks(cells), loss_part, norm, loss);
     k_tc_pack_g1<<<blocks(cells), NTT>>>(cells, g, reinterpret_cast<uint4*>(g16));
     for (int l = kLayers - 1; l >= 0; l--) {
       k_tc_grad_b<<<(unsigned)kOut[l], NTT>>>(S, kOut[l], g, gb[l]);

@@ -9,11 +9,11 @@
 // last-block counter) lives in the file-scope array below, which every GPU that loads the library
 // holds until the process exits (64 KiB of partials plus one counter).
 //
-// The arithmetic is that of the initial-volume reduction of the solver (ops 41/42,
-// coupled_motion.glslinc:356-357): sum over cells of double(F) * (double(hx)*double(hy)*double(hz)),
-// 256 cells per block, blocks reduced in a fixed tree, the last block to finish adding the
-// partials in block order — so the result is bit-identical to the solver's initial_volume_m3 for
-// the same F.
+// The arithmetic and the order of every addition are those of the solver's initial-volume
+// reduction (ops 41/42, coupled_motion.glslinc:356-357; k_init_volume through last_block_reduce):
+// per cell double(F) * (double(hx)*double(hy)*double(hz)), 256 cells per block reduced by
+// block_reduce_k, the last block to finish adding the partials with the same strided loop and
+// block_reduce_k — so the result is bit-identical to the solver's initial_volume_m3 for the same F.
 #include <mutex>
 
 #include "../../include/waves.h"
@@ -31,29 +31,102 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxBlocks + 32
 __global__ void __launch_bounds__(kNoAllocThreads)
 k_volume_noalloc(const float* __restrict__ F, long long n, double cell, double* out, double* part,
                  unsigned int* counter) {
-  __shared__ double sh[32];
+  __shared__ double sh[kNoAllocThreads];
+  __shared__ double tot[1];
   __shared__ bool am_last;
+  const int ops[1] = {0};
+  const int nb = gridDim.x;
   long long i = (long long)blockIdx.x * kNoAllocThreads + threadIdx.x;
-  double v = i < n ? (double)F[i] * cell : 0.0;
-  double r = block_reduce<kNoAllocThreads>(v, AddD(), sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = r;
+  double v[1] = {0};
+  if (i < n) v[0] = (double)F[i] * cell;
+  block_reduce_k<kNoAllocThreads, 1>(v, ops, sh, tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) am_last = atomicAdd(counter, 1u) == (unsigned)nb - 1;
   __syncthreads();
   if (!am_last) return;
   __threadfence();
-  double acc = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += kNoAllocThreads) acc += __ldcg(&part[b]);
-  double total = block_reduce<kNoAllocThreads>(acc, AddD(), sh);
+  double acc[1] = {0.0};
+  for (int b = threadIdx.x; b < nb; b += kNoAllocThreads) acc[0] = acc[0] + __ldcg(&part[b]);
+  block_reduce_k<kNoAllocThreads, 1>(acc, ops, sh, tot);
   if (threadIdx.x == 0) {
-    *out = total;
+    *out = tot[0];
     *counter = 0;
   }
 }
 
+// The scratch address is a property of a CUDA context (the module is loaded per context), so the
+// cache is keyed by device ordinal and the driver's context id, which is never reused within a
+// process: after cudaDeviceReset, or with another context current on the device, the address is
+// fetched again.  The driver's entry points are looked up through the runtime, so the library
+// does not link libcuda.  Where the driver offers no context id, the key is the ordinal alone.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
+struct ScratchEntry {
+  int dev;
+  unsigned long long ctx_id;
+  double* ptr;
+};
+constexpr int kCacheSlots = 64;
+
 std::mutex g_noalloc_mutex;
-double* g_noalloc_ptr[64] = {nullptr};
+ScratchEntry g_cache[kCacheSlots];
+int g_cache_used = 0, g_cache_next = 0;
+bool g_entry_points_tried = false;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+void* driver_entry(const char* name) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return f;
+}
+
+// Id of the context current on this thread (0 when none is current or the driver has no ids).
+unsigned long long current_context_id() {
+  if (!g_entry_points_tried) {
+    g_entry_points_tried = true;
+    g_ctx_get_current = (CtxGetCurrentFn)driver_entry("cuCtxGetCurrent");
+    g_ctx_get_id = (CtxGetIdFn)driver_entry("cuCtxGetId");
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != 0 || !ctx) return 0;
+  if (g_ctx_get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of g_noalloc_scratch in the current context of device `dev` (null on error).
+double* scratch_address(int dev) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  unsigned long long id = current_context_id();
+  if (id != 0) {
+    for (int k = 0; k < g_cache_used; k++)
+      if (g_cache[k].dev == dev && g_cache[k].ctx_id == id) return g_cache[k].ptr;
+  }
+  // Set-up: with the device current, fetch the device address of the array.  The host-side name
+  // of the array is not a device address.  This also makes the primary context current if no
+  // context was, so the id is read again afterwards.
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (id == 0) id = current_context_id();
+  int slot;
+  if (g_cache_used < kCacheSlots) slot = g_cache_used++;
+  else slot = g_cache_next = (g_cache_next + 1) % kCacheSlots;
+  g_cache[slot] = ScratchEntry{dev, id, (double*)p};
+  return (double*)p;
+}
 
 }  // namespace
 }  // namespace wg
@@ -66,22 +139,12 @@ extern "C" waves_status waves_liquid_volume_noalloc(const float* F, int32_t nx, 
   long long blocks = (n + kNoAllocThreads - 1) / kNoAllocThreads;
   if (blocks > kNoAllocMaxBlocks) return WAVES_INVALID_ARG;  // more than 2,097,152 cells
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return WAVES_NO_DEVICE;
-  double* scratch;
-  {
-    // Set-up on the first call per device, with that device current: the host-side name of the
-    // array is not a device address, so fetch the device address once and keep it.
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-        cudaGetLastError();
-        return WAVES_CUDA_ERROR;
-      }
-      g_noalloc_ptr[dev] = (double*)p;
-    }
-    scratch = g_noalloc_ptr[dev];
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+    cudaGetLastError();
+    return WAVES_NO_DEVICE;
   }
+  double* scratch = scratch_address(dev);
+  if (!scratch) return WAVES_CUDA_ERROR;
   cudaStream_t s = (cudaStream_t)stream;
   unsigned int* counter = (unsigned int*)(scratch + kNoAllocMaxBlocks);
   // The counter must start at zero; the partials are all overwritten before they are read.
