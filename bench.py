@@ -45,6 +45,11 @@ def parse():
                     help="beach: 310x48x80 (the metric's grid); large: 620x96x160, spacing halved")
     ap.add_argument("--e2e-frames", type=int, default=-1,
                     help="1/60 s frames of the end-to-end run; -1: the timed window's simulated span, 0: none")
+    ap.add_argument("--window-start", type=float, default=5.0,
+                    help="accepted time (s) the timed steps start from, reached by an untimed run from rest "
+                         "(5 s: waves developed; 0: from rest)")
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="skip the BF16-multigrid and BF16 + learned warm-start arms")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     return ap.parse_args()
@@ -108,28 +113,25 @@ def beach_config(mg, grid="beach"):
     return wg.config("beach", pressure_tolerance=TOL, mg_precision=mg, **GRIDS[grid])
 
 
-def run_ours(args, world, rank, local):
-    import torch
-    import waves_gb300 as wg
-    from waves_gb300.build import build
-    if rank == 0:
-        build()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.set_device(local)
-    cfg = beach_config(args.mg, args.grid)
-    cfg.device = local
-    s = wg.WavesSolver(cfg)
-    lib, h = s.lib, s.h
-    import ctypes as C
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+class Window:
+    """One solver handle timed over K accepted steps: every trial's device time comes from the CUDA
+    events the library records on its own stream; L2 is flushed (a 256 MiB write) before each
+    step."""
 
-    def timing(reset):
+    def __init__(self, cfg, torch, flush):
+        import ctypes as C
+        import waves_gb300 as wg
+        self.C, self.torch, self.flush = C, torch, flush
+        self.s = wg.WavesSolver(cfg)
+
+    def timing(self, reset):
+        C, s = self.C, self.s
         m, p, t = C.c_double(), C.c_double(), C.c_int64()
-        s._ck(lib.waves_timing(h, C.byref(m), C.byref(p), C.byref(t), reset))
+        s._ck(s.lib.waves_timing(s.h, C.byref(m), C.byref(p), C.byref(t), reset))
         return m.value, p.value, t.value
 
-    def one_step():
+    def one_step(self):
+        s = self.s
         c = s.control()
         target = int(c[2]) + 1
         s.request_steps(target)
@@ -141,56 +143,108 @@ def run_ours(args, world, rank, local):
             if c[7] > .5 and not ((c[7] == 20 or 10 <= c[7] <= 12) and c[29] < 2):
                 raise RuntimeError(f"solver halted with code {c[7]}")
 
-    for _ in range(max(args.warmup, 3)):
-        one_step()
-    timing(True)
-    c0 = s.control()
-    stats0 = s.stats()
-    start_state = s.save() if args.e2e_frames != 0 else None
+    def advance_to(self, t_start):
+        """Untimed run from rest to the accepted time t_start (the waves' window)."""
+        if t_start > 0:
+            self.s.request_time(t_start)
+            st = self.s.run(8)
+            if st != 0:
+                raise RuntimeError(f"solver stopped with status {st} before t = {t_start}")
+
+    def measure(self, steps, warmup, barrier=None, clocks=None):
+        s = self.s
+        for _ in range(max(warmup, 3)):
+            self.one_step()
+        self.timing(True)
+        c0, stats0 = s.control(), s.stats()
+        if barrier:
+            barrier()
+        self.torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for _ in range(steps):
+            self.flush.zero_()
+            self.torch.cuda.synchronize()
+            self.one_step()
+        wall = time.perf_counter() - wall0
+        self.torch.cuda.synchronize()
+        motion, pressure, trials = self.timing(True)
+        c1 = s.control()
+        n = max(int(c1[2] - c0[2]), 1)
+        return {"c0": c0, "c1": c1, "sim_s": c1[1] - c0[1], "device_s": (motion + pressure) / 1e3, "wall_s": wall,
+                "steps": int(c1[2] - c0[2]), "trials": trials, "motion_ms": motion, "pressure_ms": pressure,
+                "iters": c1[18] - c0[18], "rounds": (c1[32] - c0[32]) + (c1[103] - c0[103]),
+                "active": c1[32] - c0[32], "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
+                "window_s": [c0[1], c1[1]], "pressure_ms_per_step": pressure / n, "ms_per_step": (motion + pressure) / n,
+                "cg_iterations_per_step": (c1[18] - c0[18]) / n,
+                "warm_start_used": int(c1[102] - c0[102])}
+
+    def close(self):
+        self.s.close()
+
+
+def summary(r):
+    """The per-arm figures of the JSON line."""
+    return {"sim_s_per_wall_s": r["sim_s"] / r["device_s"] if r["device_s"] > 0 else None,
+            "ms_per_step": r["ms_per_step"], "pressure_ms_per_step": r["pressure_ms_per_step"],
+            "motion_ms_per_step": r["motion_ms"] / max(r["steps"], 1),
+            "cg_iterations_per_step": r["cg_iterations_per_step"], "steps": r["steps"], "trials": r["trials"],
+            "mg_builds": r["mg_builds"], "window_s": r["window_s"], "warm_start_trials": r["warm_start_used"]}
+
+
+def load_shipped_model(s):
+    """The learned warm start committed with the package (waves_gb300/learned/model_beach.npz)."""
+    import waves_gb300 as wg
+    from waves_gb300.learned import load_model
+    weights, biases, iscale, oscale = load_model(os.path.join(os.path.dirname(wg.__file__), "learned", "model_beach.npz"))
+    s.set_warm_start(weights, biases, iscale, oscale)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import waves_gb300 as wg
+    from waves_gb300.build import build
+    if rank == 0:
+        build()
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    motion = pressure = 0.0
+    torch.cuda.set_device(local)
+    import ctypes as C
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else None
+
+    def cfg_of(mg, warm=0):
+        cfg = beach_config(mg, args.grid)
+        cfg.device = local
+        cfg.warm_start = warm
+        return cfg
+
+    # the headline arm: args.mg multigrid, from the waves' window start
+    arm = Window(cfg_of(args.mg), torch, flush)
+    s, lib, h = arm.s, arm.s.lib, arm.s.h
+    arm.advance_to(args.window_start)
     with Clocks(local) as clk:
-        wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            one_step()
-        wall = time.perf_counter() - wall0
-    torch.cuda.synchronize()
-    motion, pressure, trials = timing(True)
-    c1 = s.control()
+        res = arm.measure(args.steps, args.warmup, barrier)
+    c1 = res["c1"]
     # Roofline of the dominant kernel: one further step, host-scheduled, with every launch of the
     # probed kernels bracketed by CUDA events on the solver's stream (outside the timed region).
     s.request_steps(int(c1[2]) + 1)
     probe_trials, probes = s.probe_trial()
-    sim = c1[1] - c0[1]
-    dev_s = (motion + pressure) / 1e3
     counts = (C.c_int32 * 8)()
     lib.waves_debug_launch_counts(h, counts)
     counts = list(counts)
-    active = c1[32] - c0[32]
-    rounds = active + (c1[103] - c0[103])
-    iters = c1[18] - c0[18]
+    trials, active, rounds, iters = res["trials"], res["active"], res["rounds"], res["iters"]
     # per trial: begin + condition, and when active: motion, pressure set-up, conditions, trial end;
     # per defect round: CG set-up + conditions + post; per CG iteration: the iteration kernels
     launches = int(trials * (counts[0] + counts[7] * 2) + active * (counts[1] + counts[2] + counts[6] + counts[7])
                    + rounds * (counts[3] + counts[5] + 2 * counts[7]) + iters * counts[4])
-    out = {
-        "sim_s": sim, "device_s": dev_s, "wall_s": wall, "steps": int(c1[2] - c0[2]), "trials": trials,
-        "motion_ms": motion, "pressure_ms": pressure, "iters": iters, "defect_rounds": rounds - active,
-        "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
-        "mg_builds": s.stats()["mg_builds"] - stats0["mg_builds"],
-        "probes": probes if probe_trials else [],
-        "plan": wg.mg_plan(cfg),
-    }
-    # e2e: frames through the public API with host buffers, from the state the timed steps started
-    # from (checkpoint restored), over the same simulated window unless --e2e-frames says otherwise
+    out = dict(res)
+    out.update({"defect_rounds": rounds - active, "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
+                "probes": probes if probe_trials else [], "plan": wg.mg_plan(arm.s.cfg)})
+    # e2e: frames through the public API with host buffers, over the timed steps' simulated span,
+    # from the state the solver is in now (the waves' window continues)
     e2e = None
     if args.e2e_frames != 0:
-        s.load(start_state)
-        frames = args.e2e_frames if args.e2e_frames > 0 else max(1, int(round(sim * 60.0)))
+        frames = args.e2e_frames if args.e2e_frames > 0 else max(1, int(round(res["sim_s"] * 60.0)))
         # page-locked host buffers for the per-frame surface export, as a renderer that reads the
         # surface every frame would hold them
         planes = torch.empty(4 * s.N, dtype=torch.float32, pin_memory=True).numpy()
@@ -200,15 +254,32 @@ def run_ours(args, world, rank, local):
         for f in range(frames):
             s.request_time(t_sim0 + (f + 1) / 60.0)
             s.run(4)
-            st = s.stats()
+            s.stats()
             lib.waves_export_surface(h, planes.ctypes.data_as(C.POINTER(C.c_float)), kinds.ctypes.data_as(C.POINTER(C.c_float)))
         w = time.perf_counter() - w0
         sim_e = s.control()[1] - t_sim0
-        e2e = {"sim_s": sim_e, "wall_s": w, "frames": frames,
+        e2e = {"sim_s": sim_e, "wall_s": w, "frames": frames, "window_s": [t_sim0, s.control()[1]],
                "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8)}
     out["e2e"] = e2e
     out["render"] = time_render(s, torch)
-    s.close()
+    arm.close()
+    # the same multigrid from rest (the first steps of the run: still water, forcing ramping up)
+    arms = {}
+    if args.window_start > 0:
+        rest = Window(cfg_of(args.mg), torch, flush)
+        arms["from_rest"] = summary(rest.measure(args.steps, args.warmup, barrier))
+        rest.close()
+    # the comparison the metric names: BF16 multigrid, and BF16 multigrid + learned warm start,
+    # over the same window as the headline (each from rest to the window start on its own handle)
+    if args.compare and args.grid == "beach":
+        for name, mg, warm in (("bf16", 16, 0), ("bf16_learned", 16, 1)):
+            w = Window(cfg_of(mg, warm), torch, flush)
+            if warm:
+                load_shipped_model(w.s)
+            w.advance_to(args.window_start)
+            arms[name] = summary(w.measure(args.steps, args.warmup, barrier))
+            w.close()
+    out["arms"] = arms
     return out
 
 
@@ -399,7 +470,11 @@ def main():
                                 "beach 620x96x160 (lab_runner.gd settings, spacing halved), ")
                                + ("plain FP32 MGPCG" if args.mg == 32 else "BF16 multigrid, FP32 CG") + ", tol 1e-6",
                    "cells": 1190400 if args.grid == "beach" else 9523200, "l2": "flushed between steps (256 MiB write)",
-                   "sim_window_s": [res["t_end"] - res["sim_s"], res["t_end"]],
+                   "sim_window_s": res["window_s"],
+                   "window": (f"{args.steps} accepted steps after {max(args.warmup, 3)} untimed ones, from the state an "
+                              f"untimed run from rest reached at t = {args.window_start:g} s (waves developed; the "
+                              f"forcing ramp ends at 5.6 s)") if args.window_start > 0 else
+                             f"{args.steps} accepted steps after {max(args.warmup, 3)} untimed ones from rest",
                    "parallelism": "replicas" if world > 1 else "single"},
         "pressure_ms_per_step": res["pressure_ms"] / steps,
         "motion_ms_per_step": res["motion_ms"] / steps,
@@ -426,7 +501,17 @@ def main():
         e = res["e2e"]
         line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"], "step": "one 1/60 s frame: request_time, run, stats, surface export",
-                       "frames": e["frames"], "window": "the timed steps' simulated span, from their starting state"}
+                       "frames": e["frames"], "window_s": e["window_s"],
+                       "window": "the timed steps' simulated span again, continuing from where they ended"}
+    arms = dict(res["arms"])
+    arms[("fp32" if args.mg == 32 else "bf16") + "_headline"] = summary(res)
+    line["arms"] = arms
+    plain = arms.get("fp32_headline")
+    mixed = arms.get("bf16_learned")
+    if plain and mixed:
+        # the metric's second half: pressure ms per accepted step, plain FP32 over BF16 + learned
+        line["pressure_ms_ratio_plain_fp32_over_bf16_learned"] = plain["pressure_ms_per_step"] / mixed["pressure_ms_per_step"]
+        line["sim_rate_ratio_bf16_learned_over_plain_fp32"] = mixed["sim_s_per_wall_s"] / plain["sim_s_per_wall_s"]
     if world == 1 and not args.no_cpu_baseline:
         try:
             base = cpu_baseline(args, args.mg, args.cpu_seconds, args.cpu_seconds / 2)

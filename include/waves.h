@@ -142,6 +142,9 @@ typedef struct waves_stats_t {
   int64_t mg_structure_builds;   /* structural rebuilds (state[12]) */
   int32_t mg_levels;             /* levels in the hierarchy (pressure_multigrid.gd:40-59) */
   int64_t warm_start_used;       /* trials whose initial pressure came from the learned network */
+  double staged_forcing_volume_m3;  /* c64 */
+  double staged_ocean_inflow_m3;    /* c65 */
+  double staged_ocean_outflow_m3;   /* c66 */
 } waves_stats_t;
 
 typedef struct waves_handle waves_handle;
@@ -295,6 +298,12 @@ typedef struct waves_frame_report {
   int64_t submissions_retired;
 } waves_frame_report;
 waves_status waves_frame(waves_handle* h, const waves_frame_budget* budget, waves_frame_report* report);
+/* The telemetry of the latest retired waves_frame submission, from its control-block copy: what
+ * the reference's asynchronous read-back hands to _stats (work_scheduler.gd:78-82, then
+ * pressure_gpu.gd:133-137, coupled_gpu.gd:58-65, coastal_gpu.gd:34-37).  No device access and no
+ * wait.  The hierarchy counters (mg_builds, mg_structure_builds) are those of the last
+ * waves_stats call.  WAVES_INVALID_ARG while no submission has retired. */
+waves_status waves_frame_stats(const waves_handle* h, waves_stats_t* out);
 
 /* Learned warm start (no reference counterpart): 4 layers of 3x3x3 convolutions,
  * channels 3 -> 16 -> 16 -> 16 -> 1, BF16 weights (raw uint16 bit patterns), FP32 biases.

@@ -148,14 +148,24 @@ def test_bench_json_line_contract(monkeypatch, capsys):
     bench = load_bench()
     wg.load(build_if_missing=True)
 
+    def arm(pressure_ms_per_step):
+        return {"sim_s_per_wall_s": 0.6, "ms_per_step": 12.0, "pressure_ms_per_step": pressure_ms_per_step,
+                "motion_ms_per_step": 2.0, "cg_iterations_per_step": 12.0, "steps": 240, "trials": 245,
+                "mg_builds": 60, "window_s": [5.0, 7.0], "warm_start_trials": 0}
+
     def measured(args, world, rank, local):
+        assert args.window_start == 5.0 and args.compare
         return {"sim_s": 2.0, "device_s": 3.0, "wall_s": 3.1, "steps": 240, "trials": 245, "motion_ms": 500.0,
                 "pressure_ms": 2500.0, "iters": 3103.0, "defect_rounds": 1, "launches": 123456,
-                "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}, "t_end": 2.04, "mg_builds": 63,
+                "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}, "t_end": 7.0, "mg_builds": 63,
                 "probes": [{"kernel": "k_mgl_rows", "launches": 100, "ms": 1.5, "bytes": 100 * 8e6},
                            {"kernel": "all", "launches": 900, "ms": 11.0, "bytes": 0.0}],
-                "plan": wg.mg_plan(wg.config("beach")),
-                "e2e": {"sim_s": 2.0, "wall_s": 3.2, "frames": 120, "h2d": 8, "d2h": 23809032}, "render": None}
+                "plan": wg.mg_plan(wg.config("beach")), "window_s": [5.0, 7.0],
+                "ms_per_step": 12.5, "pressure_ms_per_step": 2500.0 / 240, "cg_iterations_per_step": 3103.0 / 240,
+                "warm_start_used": 0,
+                "arms": {"from_rest": arm(8.0), "bf16": arm(10.0), "bf16_learned": arm(12.5)},
+                "e2e": {"sim_s": 2.0, "wall_s": 3.2, "frames": 120, "h2d": 8, "d2h": 23809032, "window_s": [7.0, 9.0]},
+                "render": None}
 
     monkeypatch.setattr(bench, "run_ours", measured)
     monkeypatch.setattr(sys, "argv", ["bench.py", "--no-cpu-baseline"])
@@ -174,20 +184,33 @@ def test_bench_json_line_contract(monkeypatch, capsys):
     step = bench.step_bytes_model(wg.mg_plan(wg.config("beach")), 3103.0 / 240, 63 / 240, False)
     assert d["step_roofline"]["bytes_per_step"] == pytest.approx(step["bytes_per_step"])
     assert d["e2e"]["value"] == pytest.approx(2.0 / 3.2) and d["e2e"]["d2h_bytes_per_step"] == 23809032
+    # the metric's second half: pressure ms per step of plain FP32 against BF16 + learned warm start
+    assert set(d["arms"]) == {"from_rest", "bf16", "bf16_learned", "fp32_headline"}
+    assert d["pressure_ms_ratio_plain_fp32_over_bf16_learned"] == pytest.approx((2500.0 / 240) / 12.5)
+    assert d["config"]["sim_window_s"] == [5.0, 7.0] and "t = 5 s" in d["config"]["window"]
 
 
 def test_gdscript_mirror_frame_packet_and_quota_without_a_gpu():
-    """waves_gb300.gd: request(steps) is a positive accepted-step quota and request_time(t) a
-    negative deadline (pressure_gpu.gd:48-54), forwarded before every frame; the frame's telemetry
-    packet carries the work_scheduler.gd:40,86 keys; frame() is False once idle or halted, and a
-    closed solver does nothing.  The solver is a fake standing in for the CUDA one."""
+    """The mirror's frame() against a fake solver: quota forwarding, the budget defaults of
+    work_scheduler.gd, and the packets lab_runner.gd:_process (:49-60) reads after merging them
+    (:29-31): accepted_steps, accepted_time, pending, failure (recoverable codes masked, as
+    coupled_gpu.gd:61-62), replayed here the way the GDScript does."""
+    from waves_gb300.abi import WavesStats
     from waves_gb300.gd import CoastalGPU
+
+    def control_stats(steps, time, pending, failure, trial_failure, retries):
+        st = WavesStats().as_dict()
+        st.update(accepted_steps=steps, accepted_time=time, pending=pending, failure=failure,
+                  trial_failure=trial_failure, retry_count=retries, trial_count=steps + 1)
+        return st
 
     class Fake:
         def __init__(self):
             self.calls = []
             self.report = {"trials_submitted": 3, "queue_depth": 2, "predicted_gpu_ms": 1.5, "gpu_ms_total": 4.0,
-                           "r_fluid": 0.9, "accepted_steps": 7, "accepted_time": 0.05, "idle": 0, "halted": 0}
+                           "r_fluid": 0.9, "accepted_steps": 7, "accepted_time": 0.05, "idle": 0, "halted": 0,
+                           "submissions_retired": 1}
+            self.retired = control_stats(7, 0.05, 1, 0, 0, 0)
 
         def request_steps(self, n):
             self.calls.append(("steps", n))
@@ -199,6 +222,12 @@ def test_gdscript_mirror_frame_packet_and_quota_without_a_gpu():
             self.calls.append(("frame", budget))
             return dict(self.report)
 
+        def frame_stats(self):
+            return dict(self.retired)
+
+        def device_bytes(self):
+            return 1234
+
         def close(self):
             self.calls.append(("close",))
 
@@ -206,19 +235,73 @@ def test_gdscript_mirror_frame_packet_and_quota_without_a_gpu():
     g = CoastalGPU({"n": (310, 48, 80)})
     g.connect(packets.append)
     g.solver = fake = Fake()
-    g.request_time(1.0)
+
+    # lab_runner.gd state and _process, on the merged telemetry dictionary
+    lab = {"stats": {}, "requested": 0, "requested_time": 0.0, "single_pending": False, "paused": False}
+
+    def on_packet(p):
+        lab["stats"].update(p)
+    g.connect(on_packet)
+
+    def process(wall_time):
+        stats = lab["stats"]
+        lab["requested_time"] = wall_time
+        completed = stats.get("accepted_steps", stats.get("steps", 0))
+        elapsed = stats.get("accepted_time", completed / 120.0)
+        if lab["single_pending"] and completed >= lab["requested"]:
+            lab["single_pending"] = False
+            lab["requested_time"] = max(lab["requested_time"], elapsed)
+        if not lab["paused"] and stats.get("failure", 0) == 0:
+            g.request_time(lab["requested_time"])
+        status = "PAUSED" if lab["paused"] else "RUNNING"
+        if lab["paused"] and (stats.get("pending", False) or lab["single_pending"]):
+            status = "PAUSING"
+        if stats.get("failure", 0) > 0:
+            status = "STOPPED"
+        return status, completed, elapsed
+
+    assert process(1.0) == ("RUNNING", 0, 0.0)
     assert g.frame() is True
     assert fake.calls[0] == ("time", 1.0) and fake.calls[1][0] == "frame"
     assert fake.calls[1][1] == {"gpu_budget_ms": 14.0, "max_inflight": 3, "max_trials": 96, "cpu_budget_ms": 4.0}
-    p = packets[-1]
-    assert p["submission_chunks"] == 3 and p["queue_depth"] == 2 and p["R_fluid"] == 0.9 and p["failure"] == 0
-    assert p["predicted_gpu_ns"] == pytest.approx(1.5e6) and p["gpu_ns"] == pytest.approx(4.0e6)
-    assert p["submission_accepted_steps"] == 7 and g.last_stats["accepted_time"] == 0.05
+    stats = lab["stats"]
+    assert stats["accepted_steps"] == 7 and stats["accepted_time"] == 0.05 and stats["pending"] is True
+    assert stats["failure"] == 0 and stats["coupled"] is True and stats["allocated_bytes"] == 1234
+    assert stats["submission_chunks"] == 3 and stats["queue_depth"] == 2 and stats["submission_accepted_steps"] == 7
+    assert stats["gpu_ns"] == pytest.approx(4.0e6) and stats["R_fluid"] == pytest.approx(4.0e-3 / 0.05)
+    assert "gauges_m" in stats and "forcing_momentum_kg_mps" in stats and "staged_forcing_volume_m3" in stats
+    assert process(1.1) == ("RUNNING", 7, 0.05)
+
+    # pause with a trial pending, then single-step: N requests accepted_steps + 1 (lab_runner.gd:64-72)
+    lab["paused"] = True
+    g.request(stats["accepted_steps"])
+    assert process(1.2)[0] == "PAUSING"
+    lab["requested"] = stats["accepted_steps"] + 1
+    lab["single_pending"] = True
+    g.request(lab["requested"])
+    fake.report.update(submissions_retired=2)
+    fake.retired = control_stats(8, 0.0583, 0, 0, 0, 0)
+    g.frame()
+    assert ("steps", 8) in fake.calls
+    assert process(1.3) == ("PAUSED", 8, 0.0583) and lab["single_pending"] is False
+
+    # a recoverable trial failure (code 11 with retries left) reads 0; a halt reads the code
+    lab["paused"] = False
+    fake.report.update(submissions_retired=3)
+    fake.retired = control_stats(8, 0.0583, 1, 0, 11, 1)
+    g.frame()
+    assert stats["failure"] == 0 and stats["trial_failure"] == 11 and process(1.4)[0] == "RUNNING"
+    fake.report.update(submissions_retired=4, halted=1)
+    fake.retired = control_stats(8, 0.0583, 0, 4, 4, 0)
+    assert g.frame() is False
+    assert stats["failure"] == 4 and process(1.5)[0] == "STOPPED"
+    # no new retirement: no new _stats packet, only the cost packet
+    n = len(packets)
+    g.frame()
+    assert len(packets) == n + 1 and set(packets[-1]) == {"record_us", "gpu_ns", "R_fluid"}
     g.request(12)
     fake.report["idle"] = 1
     assert g.frame() is False and ("steps", 12) in fake.calls
-    fake.report.update(idle=0, halted=1)
-    assert g.frame() is False and packets[-1]["failure"] == 1
     with pytest.raises(AssertionError):
         g.request_time(float("nan"))
     g.close()

@@ -39,8 +39,8 @@ def test_liquid_volume_noalloc_matches_solver_twice(gpu_lib):
         st, v = _volume(gpu_lib, F, n, h, out)
         assert st == 0
         assert v == v0, (v, v0)  # the solver's reduction order: equal bits
-    # a ragged size (the first (nx-1)*ny*nz cells: not a multiple of the 256-cell block)
-    ragged = (n[0] - 1, n[1], n[2])
+    # a ragged size (the first nx*ny*(nz-1) cells: not a multiple of the 256-cell block)
+    ragged = (n[0], n[1], n[2] - 1)
     count = ragged[0] * ragged[1] * ragged[2]
     assert count % 256 != 0
     cell = float(np.float32(h[0])) * float(np.float32(h[1])) * float(np.float32(h[2]))

@@ -130,6 +130,20 @@ class WavesSolver:
         self._ck(self.lib.waves_frame(self.h, C.byref(b), C.byref(r)))
         return r.as_dict()
 
+    def frame_stats(self):
+        """Telemetry of the latest retired frame submission (waves_frame_stats): no device access,
+        no wait.  None while no submission has retired."""
+        s = WavesStats()
+        if self.lib.waves_frame_stats(self.h, C.byref(s)) != 0:
+            return None
+        return s.as_dict()
+
+    def device_bytes(self):
+        """Bytes of the handle's persistent device state (the size waves_save reports)."""
+        n = C.c_size_t(0)
+        self._ck(self.lib.waves_save(self.h, None, C.byref(n)))
+        return int(n.value) - 16
+
     def synchronize(self):
         self._ck(self.lib.waves_synchronize(self.h))
 

@@ -112,6 +112,9 @@ class WavesStats(C.Structure):
         ("mg_structure_builds", C.c_int64),
         ("mg_levels", C.c_int32),
         ("warm_start_used", C.c_int64),
+        ("staged_forcing_volume_m3", C.c_double),
+        ("staged_ocean_inflow_m3", C.c_double),
+        ("staged_ocean_outflow_m3", C.c_double),
     ]
 
     def as_dict(self):
@@ -221,6 +224,7 @@ WAVES_ABI_SYMBOLS = [
     "waves_request_time",
     "waves_advance",
     "waves_frame",
+    "waves_frame_stats",
     "waves_run",
     "waves_synchronize",
     "waves_stream",
@@ -269,6 +273,7 @@ def declare(lib):
         "waves_advance": (C.c_int, [h, C.c_int32]),
         "waves_run": (C.c_int, [h, C.c_int32]),
         "waves_frame": (C.c_int, [h, P(WavesFrameBudget), P(WavesFrameReport)]),
+        "waves_frame_stats": (C.c_int, [h, P(WavesStats)]),
         "waves_synchronize": (C.c_int, [h]),
         "waves_stream": (C.c_void_p, [h]),
         "waves_timing": (C.c_int, [h, P(C.c_double), P(C.c_double), P(C.c_int64), C.c_int32]),

@@ -93,6 +93,7 @@ struct waves_handle {
   double* frame_c = nullptr;  // pinned, kFrameSlots x WAVES_CONTROL_SIZE
   double last_c[WAVES_CONTROL_SIZE] = {};
   bool have_last = false;
+  int64_t last_mg_builds = 0, last_mg_structure_builds = 0;  // hierarchy counters of the last waves_stats
   int64_t serial = 0, retired = 0;
 };
 
@@ -1119,13 +1120,9 @@ waves_status waves_inject_rejection(waves_handle* h) {
   return WAVES_OK;
 }
 
-waves_status waves_stats(waves_handle* h, waves_stats_t* o) {
-  if (!h || !o) return WAVES_INVALID_ARG;
-  waves_status st;
-  if ((st = read_control(h)) != WAVES_OK) return st;
-  unsigned hs[16];
-  CK(cudaMemcpy(hs, h->D.hstate, sizeof(hs), cudaMemcpyDeviceToHost));
-  const double* v = h->host_c;
+// Telemetry fields that come from the control block (pressure_gpu.gd:133-137, coupled_gpu.gd:58-65,
+// coastal_gpu.gd:34-37): recoverable trial failures read 0 in `failure` (coupled_gpu.gd:61-62).
+static void stats_from_control(const double* v, waves_stats_t* o) {
   std::memset(o, 0, sizeof(*o));
   bool recoverable = (v[7] == 20 || (v[7] >= 10 && v[7] <= 12)) && v[29] < 2;
   o->accepted_index = (int32_t)v[0];
@@ -1171,10 +1168,34 @@ waves_status waves_stats(waves_handle* h, waves_stats_t* o) {
   o->forcing_min_F = v[88];
   o->forcing_max_F = v[89];
   o->conservation_residual_m3 = v[wg::kConservation];
+  o->staged_forcing_volume_m3 = v[64];
+  o->staged_ocean_inflow_m3 = v[65];
+  o->staged_ocean_outflow_m3 = v[66];
+  o->warm_start_used = (int64_t)v[wg::kWarmUsed];
+}
+
+waves_status waves_stats(waves_handle* h, waves_stats_t* o) {
+  if (!h || !o) return WAVES_INVALID_ARG;
+  waves_status st;
+  if ((st = read_control(h)) != WAVES_OK) return st;
+  unsigned hs[16];
+  CK(cudaMemcpy(hs, h->D.hstate, sizeof(hs), cudaMemcpyDeviceToHost));
+  stats_from_control(h->host_c, o);
   o->mg_builds = hs[11];
   o->mg_structure_builds = hs[12];
   o->mg_levels = h->D.L;
-  o->warm_start_used = (int64_t)v[wg::kWarmUsed];
+  h->last_mg_builds = hs[11];
+  h->last_mg_structure_builds = hs[12];
+  return WAVES_OK;
+}
+
+waves_status waves_frame_stats(const waves_handle* h, waves_stats_t* o) {
+  if (!h || !o) return WAVES_INVALID_ARG;
+  if (!h->have_last) return WAVES_INVALID_ARG;
+  stats_from_control(h->last_c, o);
+  o->mg_builds = h->last_mg_builds;
+  o->mg_structure_builds = h->last_mg_structure_builds;
+  o->mg_levels = h->D.L;
   return WAVES_OK;
 }
 

@@ -13,12 +13,59 @@ water/pressure_gpu.gd, water/coupled_gpu.gd and water/coastal_gpu.gd expose to t
 
 These classes keep those names and semantics over the C ABI.  `frame()` plays the role of the
 render-thread work of work_scheduler.gd:41-87: one budgeted submission per call (waves_frame),
-never a wait for the GPU, and one telemetry packet; `run()` submits until the quota is met.  The
-settings dictionary uses the keys of lab_runner.gd:26.
+never a wait for the GPU; when a submission has retired, the telemetry of its control-block copy is
+emitted as the reference's _stats packets (pressure_gpu.gd:133-137, coupled_gpu.gd:58-65,
+coastal_gpu.gd:34-37, with their key names), followed by the submission packet
+(work_scheduler.gd:82) and the cost packet (:40).  `run()` submits until the quota is met and emits
+the same _stats packets.  The settings dictionary uses the keys of lab_runner.gd:26.
 """
 import math
 
 from . import WavesSolver, config
+
+
+def stats_packets(st, coastal, record_us=0.0, gpu_ns=0.0, batches_last_frame=0, iterations_per_batch=8,
+                  transport_cache=True, allocated_bytes=0):
+    """The packets the reference's _stats chain emits for one control-block read-back, built from a
+    waves_stats_t dict: pressure_gpu.gd:135 (failure masked for recoverable codes, as
+    coupled_gpu.gd:61-62 passes it on), coupled_gpu.gd:64 and, for the coastal class,
+    coastal_gpu.gd:37."""
+    t = st["accepted_time"]
+    pressure = {"pressure_backend": "multigrid", "batches_last_frame": batches_last_frame,
+                "iterations_per_batch": iterations_per_batch, "accepted_index": int(st["accepted_index"]),
+                "accepted_time": t, "accepted_steps": int(st["accepted_steps"]), "rejections": int(st["rejections"]),
+                "pending": bool(st["pending"]), "converged": bool(st["converged"]), "failure": int(st["failure"]),
+                "iterations": int(st["iterations"]), "relative_residual": st["relative_residual"],
+                "max_dt_divergence": st["max_dt_divergence"], "max_face_speed": st["max_face_speed"],
+                "hydrostatic_error_pa": st["hydrostatic_error_pa"], "volume_m3": st["volume_m3"],
+                "total_iterations": int(st["total_iterations"]), "record_us": record_us, "gpu_ns": gpu_ns,
+                "R_fluid": gpu_ns / 1e9 / t if t > 0 else -1}
+    coupled = {"transport_cache": bool(transport_cache),
+               "rhs_integrated_divergence_l2": st["rhs_integrated_divergence_l2"],
+               "residual_integrated_divergence_l2": st["residual_integrated_divergence_l2"],
+               "true_relative_residual": st["true_relative_residual"],
+               "pressure_defect_corrections": int(st["pressure_defect_corrections"]),
+               "boundary_outflow_m3": st["boundary_outflow_m3"], "tentative_outflow_m3": st["tentative_outflow_m3"],
+               "raw_compression_volume_m3": st["raw_compression_volume_m3"],
+               "compression_volume_m3": st["compression_volume_m3"],
+               "compression_coverage_errors": int(st["compression_coverage_errors"]),
+               "step_start_volume_m3": st["step_start_volume_m3"], "trial_count": int(st["trial_count"]),
+               "trial_failure": int(st["trial_failure"]), "retry_count": int(st["retry_count"]),
+               "last_rejection_code": int(st["last_rejection_code"]), "last_rejected_dt": st["last_rejected_dt"],
+               "dt": st["dt"], "signed_roundoff_m3": st["signed_roundoff_m3"],
+               "absolute_roundoff_m3": st["absolute_roundoff_m3"], "max_CFL": st["max_CFL"],
+               "mass_defect_m3": st["mass_defect_m3"], "initial_volume_m3": st["initial_volume_m3"], "coupled": True,
+               "allocated_bytes": allocated_bytes}
+    out = [pressure, coupled]
+    if coastal:
+        out.append({"forcing_min_F": st["forcing_min_F"], "forcing_max_F": st["forcing_max_F"],
+                    "forcing_volume_m3": st["forcing_volume_m3"], "ocean_inflow_m3": st["ocean_inflow_m3"],
+                    "ocean_outflow_m3": st["ocean_outflow_m3"],
+                    "forcing_momentum_kg_mps": list(st["forcing_momentum"]),
+                    "staged_forcing_volume_m3": st["staged_forcing_volume_m3"],
+                    "staged_ocean_inflow_m3": st["staged_ocean_inflow_m3"],
+                    "staged_ocean_outflow_m3": st["staged_ocean_outflow_m3"], "gauges_m": list(st["gauges_m"])})
+    return out
 
 
 def settings_to_config(settings, coastal):
@@ -73,6 +120,10 @@ class PressureGPU:
         self.planes = None
         self.kinds = None
         self.last_stats = {}
+        self._retired = 0
+        self._submission = 0
+        self._max_queue = 0
+        self._record_us = 0.0
 
     # signal telemetry(packet: Dictionary)
     def connect(self, callback):
@@ -96,23 +147,53 @@ class PressureGPU:
     def frame(self, gpu_budget_ms=14.0, max_inflight=3, max_trials=96, cpu_budget_ms=4.0):
         """One rendered frame of water/work_scheduler.gd:frame through waves_frame: trials toward the
         current quota within the GPU and CPU budgets, at most max_inflight unfinished submissions,
-        never a wait for the GPU; emits the frame's telemetry (work_scheduler.gd:40,86 keys).
+        never a wait for the GPU.  When a submission has retired since the last frame, its
+        telemetry is emitted as the _stats packets, then the submission packet
+        (work_scheduler.gd:82 keys) and the cost packet (work_scheduler.gd:40 keys).
         Returns False once the quota is met with nothing in flight, or the solver halted."""
+        import time
         if self.solver is None or self.closed:
             return False
         if self._target >= 0:
             self.solver.request_steps(int(self._target))
         else:
             self.solver.request_time(-self._target)
+        t0 = time.perf_counter()
         r = self.solver.frame(gpu_budget_ms=gpu_budget_ms, max_inflight=max_inflight, max_trials=max_trials,
                               cpu_budget_ms=cpu_budget_ms)
-        packet = {"submission_chunks": r["trials_submitted"], "queue_depth": r["queue_depth"],
-                  "predicted_gpu_ns": r["predicted_gpu_ms"] * 1e6, "gpu_ns": r["gpu_ms_total"] * 1e6,
-                  "R_fluid": r["r_fluid"], "submission_accepted_steps": r["accepted_steps"],
-                  "submission_accepted_time": r["accepted_time"], "failure": r["halted"]}
-        self.last_stats.update({"accepted_steps": r["accepted_steps"], "accepted_time": r["accepted_time"]})
-        self._emit(packet)
+        record_us = (time.perf_counter() - t0) * 1e6
+        self._record_us += record_us
+        if r["trials_submitted"] > 0:
+            self._submission += 1
+        self._max_queue = max(self._max_queue, r["queue_depth"])
+        gpu_ns = r["gpu_ms_total"] * 1e6
+        if r["submissions_retired"] > self._retired:
+            self._retired = r["submissions_retired"]
+            st = self.solver.frame_stats()
+            if st is not None:
+                for packet in stats_packets(st, self.coastal, record_us=self._record_us, gpu_ns=gpu_ns,
+                                            batches_last_frame=r["trials_submitted"],
+                                            iterations_per_batch=int(self.config.get("iterations_per_batch", 8)),
+                                            transport_cache=self.config.get("transport_cache", True),
+                                            allocated_bytes=self._allocated()):
+                    self.last_stats.update(packet)
+                    self._emit(packet)
+                self._emit({"submission_id": self._submission, "submission_chunks": r["trials_submitted"],
+                            "submission_accepted_steps": int(st["accepted_steps"]),
+                            "submission_accepted_time": st["accepted_time"],
+                            "submission_iterations": int(st["iterations"]), "queue_depth": r["queue_depth"],
+                            "maximum_queue_depth": self._max_queue, "record_us_submission": record_us,
+                            "predicted_gpu_ns": r["predicted_gpu_ms"] * 1e6, "work_schedule": "trials"})
+        elapsed = self.last_stats.get("accepted_time", 0.0)
+        self._emit({"record_us": self._record_us, "gpu_ns": gpu_ns,
+                    "R_fluid": gpu_ns / 1e9 / elapsed if elapsed > 0 else -1})
         return not (r["idle"] or r["halted"])
+
+    def _allocated(self):
+        try:
+            return self.solver.device_bytes()
+        except Exception:
+            return 0
 
     def run(self, trials_per_sync=4):
         if self._target >= 0:
@@ -120,8 +201,12 @@ class PressureGPU:
         else:
             self.solver.request_time(-self._target)
         self.solver.run(trials_per_sync)
-        self.last_stats = self.solver.stats()
-        self._emit(self.last_stats)
+        st = self.solver.stats()
+        for packet in stats_packets(st, self.coastal, iterations_per_batch=int(self.config.get("iterations_per_batch", 8)),
+                                    transport_cache=self.config.get("transport_cache", True),
+                                    allocated_bytes=self._allocated()):
+            self.last_stats.update(packet)
+            self._emit(packet)
         return self.last_stats
 
     def export(self):
