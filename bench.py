@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--window-start", type=float, default=5.0,
                     help="accepted time (s) the timed steps start from, reached by an untimed run from rest "
                          "(5 s: waves developed; 0: from rest)")
+    ap.add_argument("--host-window", action="store_true",
+                    help="time the window on a host-scheduled handle that takes over the graph run's checkpoint at "
+                         "the window start (every kernel launched one by one, visible to kernel profilers)")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip the BF16-multigrid and BF16 + learned warm-start arms")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -220,8 +223,21 @@ def run_ours(args, world, rank, local):
 
     # the headline arm: args.mg multigrid, from the waves' window start
     arm = Window(cfg_of(args.mg), torch, flush)
-    s, lib, h = arm.s, arm.s.lib, arm.s.h
     arm.advance_to(args.window_start)
+    if args.host_window:
+        checkpoint = arm.s.save()
+        arm.close()
+        previous = os.environ.get("WAVES_SCHEDULE")
+        os.environ["WAVES_SCHEDULE"] = "host"
+        try:
+            arm = Window(cfg_of(args.mg), torch, flush)
+        finally:
+            if previous is None:
+                del os.environ["WAVES_SCHEDULE"]
+            else:
+                os.environ["WAVES_SCHEDULE"] = previous
+        arm.s.load(checkpoint)
+    s, lib, h = arm.s, arm.s.lib, arm.s.h
     with Clocks(local) as clk:
         res = arm.measure(args.steps, args.warmup, barrier)
     c1 = res["c1"]

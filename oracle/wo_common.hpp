@@ -10,10 +10,11 @@
 // Reductions always accumulate in double.  Transcendentals are evaluated in double and rounded
 // to R, in the oracle and in the kernels alike.
 //
-// Parity status: the reference has no tests, golden vectors or fixtures, so this oracle's parity
-// with the reference is UNPINNED by reference tests; it is checked against the analytic known
-// answers the shaders encode (PLIC identities, still-water hydrostatics, dispersion relation,
-// Stokes probe formulas) in tests/test_oracle_kat.py.
+// Parity status: the reference has no tests, golden vectors or fixtures.  This oracle is pinned to
+// the reference's own GLSL compute shaders, translated to C++ and run on the host beside it, op by
+// op (oracle/glsl/, tests/test_cpu_reference_pin.py), and to the analytic known answers the shaders
+// encode (PLIC identities, still-water hydrostatics, dispersion relation, Stokes probe formulas) in
+// tests/test_cpu_oracle.py.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may build or call this.
 #pragma once
