@@ -346,25 +346,35 @@ def ncu_traffic():
 
 def roofline(probes):
     """HBM roofline of the kernel with the largest probed time in one trial: algorithmic bytes per
-    launch / CUDA-event time per launch, against the measured copy bandwidth."""
-    live = [p for p in probes if p["launches"] > 0 and p["ms"] > 0 and p["kernel"] != "all"]
+    launch / CUDA-event time per launch, against the measured copy bandwidth.  Each probed launch
+    carries two nested event brackets; their cost per launch, measured on an empty kernel
+    bracketed the same way (the 'empty' calibration), is taken off every probed launch (at most
+    down to a tenth of its bracketed time), so short kernels are not ranked by the bracket."""
+    cal = {p["kernel"]: p for p in probes}
+    empty = cal.get("empty")
+    bracket_us = 1e3 * empty["ms"] / empty["launches"] if empty and empty["launches"] else 0.0
+    live = [p for p in probes if p["launches"] > 0 and p["ms"] > 0 and p["kernel"] not in ("all", "empty", "empty_inner")]
     if not live:
         return None, []
     peak, source = measured_peaks()
-    total = sum(p["ms"] for p in live)
     table = []
     for p in live:
-        gbs = p["bytes"] / (p["ms"] / 1e3) / 1e9
-        table.append({"kernel": p["kernel"], "launches": p["launches"], "us_per_launch": 1e3 * p["ms"] / p["launches"],
-                      "bytes_per_launch": p["bytes"] / p["launches"], "achieved_gbs": gbs, "frac": gbs / peak,
-                      "share_of_probed": p["ms"] / total})
+        raw_us = 1e3 * p["ms"] / p["launches"]
+        us = max(raw_us - bracket_us, 0.1 * raw_us)
+        gbs = p["bytes"] / p["launches"] / (us / 1e6) / 1e9
+        table.append({"kernel": p["kernel"], "launches": p["launches"], "us_per_launch": us, "us_per_launch_bracketed": raw_us,
+                      "bytes_per_launch": p["bytes"] / p["launches"], "achieved_gbs": gbs, "frac": gbs / peak})
+    total = sum(t["us_per_launch"] * t["launches"] for t in table)
+    for t in table:
+        t["share_of_probed"] = t["us_per_launch"] * t["launches"] / total
     top = max(table, key=lambda t: t["us_per_launch"] * t["launches"])
     traffic = ncu_traffic().get(top["kernel"])
     return {"bound": "hbm", "kernel": top["kernel"], "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
             "frac": top["frac"], "peak_source": f"{source} copy bandwidth (hbm_gbs)",
             "traffic": traffic, "bytes_per_launch": top["bytes_per_launch"], "us_per_launch": top["us_per_launch"],
             "launches": top["launches"],
-            "timing": "CUDA events on the solver stream around each launch, one host-scheduled trial after the timed steps"}, table
+            "timing": "CUDA events on the solver stream around each launch, one host-scheduled trial after the timed steps, "
+                      f"less the {bracket_us:.2f} us per launch the brackets measure on an empty kernel"}, table
 
 
 STEP_BYTES_FORMULA = ("152 N + builds/step * (28 N + sum_{l>=1} S_l n_l b_m) + CG iterations/step * "

@@ -47,6 +47,16 @@ def test_bench_roofline_picks_the_largest_probed_time():
     assert roof["frac"] == pytest.approx(roof["achieved"] / peak)
     assert sum(t["share_of_probed"] for t in table) == pytest.approx(1.0)
     assert bench.roofline([]) == (None, [])
+    # with the bracket calibration (8 us per bracketed empty launch) the ten short launches of
+    # k_a (50 us each bracketed -> 42 us) outweigh the two long ones of k_b (500 -> 492 us)? no:
+    # 10 x 42 = 420 < 2 x 492 = 984; k_b stays on top, and each time loses the bracket
+    cal = probes + [{"kernel": "empty", "launches": 64, "ms": 64 * 0.008, "bytes": 0.0},
+                    {"kernel": "empty_inner", "launches": 64, "ms": 64 * 0.004, "bytes": 0.0}]
+    roof, table = bench.roofline(cal)
+    a = next(t for t in table if t["kernel"] == "k_a")
+    assert roof["kernel"] == "k_b" and roof["us_per_launch"] == pytest.approx(492.0)
+    assert a["us_per_launch"] == pytest.approx(42.0) and a["us_per_launch_bracketed"] == pytest.approx(50.0)
+    assert roof["achieved"] == pytest.approx(100e6 / 492e-6 / 1e9)
 
 
 def test_mg_plan_of_the_beach_and_the_large_grid():

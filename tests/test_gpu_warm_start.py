@@ -49,8 +49,13 @@ def reference(F, b, p, kind, n, weights, biases, iscale, oscale):
 
 
 @pytest.mark.gpu
-def test_network_matches_fp32_reference(gpu_lib):
-    cfg = beach_slope(warm_start=1)
+@pytest.mark.parametrize("form,nx", [("tcgen05", 64), ("tcgen05", 200), ("sync", 64)])
+def test_network_matches_fp32_reference(gpu_lib, monkeypatch, form, nx):
+    """Both forms of the layers (tcgen05 with tensor-memory accumulators, the default; mma.sync):
+    one block row of 128 cells partly past the grid's x extent (64 cells) and one spanning two
+    blocks (200)."""
+    monkeypatch.setenv("WAVES_NET_MMA", form)
+    cfg = wg.config("beach", n=(nx, 40, 8), origin=(0.5, -0.6, -0.2), warm_start=1)
     s = wg.WavesSolver(cfg)
     weights, biases = random_model(7)
     iscale, oscale = (1.0, 1e-3, 1e-3), 10.0

@@ -38,6 +38,7 @@ struct MGLevelDev {
   int soff;          // offset of this level's stencil in the stencil table
   int roff[3];       // restriction tables of this (coarse) level, per axis (4 entries per coarse index)
   int rext[3];       // entries used per coarse index, per axis
+  int gal_slots;     // > 0: Galerkin partials of this (coarse) level kept per stencil entry (gal_cslot)
 };
 
 struct Dev {
@@ -111,16 +112,24 @@ struct Dev {
   const signed char* clear_tab;  // 1 when no solid cell lies in the 3x3 (x, y) window
   const unsigned char* mac_class;  // per (axis, y, x) face column: 1 near a solid cell or the domain edge
   unsigned char* ext_nb;         // per face: wall bit and usable extension neighbours (static)
+  const signed char* gal_cslot;  // per level, 125 box slots -> stencil entry (-1: not in the stencil)
   int* mac_list;                 // MacCormack work list (faces)
-  unsigned* mac_ctr;             // interior count, boundary count, op 27 / op 28 cursors
+  unsigned* mac_ctr;             // kMacCounters: interior count, boundary count, op 27 / op 28 cursors of
+                                 // the general pass, op 27 / op 28 cursors of the fast pass, op 27 / op 28
+                                 // counts of faces the fast pass handed over
+  int* mac_ovf;                  // faces the fast pass handed over to the general pass
   int mac_grid;                  // persistent MacCormack blocks (3 per SM form)
   int mac_grid2;                 // the same, 2 per SM form
+  int mac_fast_grid;             // persistent blocks of the interior fast-path pass
   int mac_minb;                  // which form runs (2 or 3 blocks per SM)
+  int mac_split;                 // interior faces on the fast-path pass
   int pdl_early;                 // kernels trigger their dependents' launch on entry
   // learned warm start (allocated when warm_start is configured): weights in mma fragment order,
   // biases [4][16], scales (F, b, p_prev inputs; output), BF16 activations [2][N][16], p_net [N]
   int net_on;
   uint32_t* net_w;
+  uint16_t* net_wt;  // the same weights for the tcgen05 layers: [layer][tap][channel half][co][8 ci] BF16
+  int net_tc05;      // 1: network layers on tcgen05 (else mma.sync)
   float* net_b;
   float* net_scale;
   unsigned short* net_act;

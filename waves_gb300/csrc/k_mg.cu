@@ -461,15 +461,21 @@ DI void child_range(const Dev& D, int l, int axis, int qc, int& lo, int& ext) {
 template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __grid_constant__ Dev D, int l, int ex, int ey, int ez) {
   grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
-  extern __shared__ float part[];  // [125][GT]
+  // [slots][GT]: one slot per offset of the 5x5x5 box, or one per stencil entry of the coarse level
+  // (gal_slots > 0; the slot map is the same for every row, so each slot's terms are added in the
+  // same order either way)
+  extern __shared__ float part[];
   MG m(D);
   const int G = ey * ez, rpb = GT / G;
   const MGLevelDev& fl = D.lv[l];
   const MGLevelDev& cl = D.lv[l + 1];
   const int t = threadIdx.x;
+  const int nslots = cl.gal_slots > 0 ? cl.gal_slots : 125;
   __shared__ I3 offs[kMaxStencil];
+  __shared__ signed char cslot[125];
   for (int k = t; k < fl.stencil; k += GT) offs[k] = m.offset(l, k);
-  for (int s = 0; s < 125; s++) part[s * GT + t] = 0.f;
+  for (int s = t; s < 125; s += GT) cslot[s] = cl.gal_slots > 0 ? D.gal_cslot[(l + 1) * 125 + s] : (signed char)s;
+  for (int s = 0; s < nslots; s++) part[s * GT + t] = 0.f;
   __syncthreads();
   int row_local = t / G, g = t % G;
   int I = blockIdx.x * rpb + row_local;
@@ -542,8 +548,9 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
           const bool ub = use && wv[b] > 0.f;
           const I3 d = m.delta_q(l + 1, qc, MG::unpack(qv[b]));
           const bool far = abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2;
-          if (ub && far) D.c[7] = 31;
-          if (ub && !far) part[MG::slot(d) * GT + t] += al * wv[b];
+          const int cs = far ? -1 : cslot[MG::slot(d)];
+          if (ub && (far || cs < 0)) D.c[7] = 31;
+          if (ub && cs >= 0) part[cs * GT + t] += al * wv[b];
         }
       }
     }
@@ -554,7 +561,9 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
     int row = blockIdx.x * rpb + rl;
     if (row >= cl.count) continue;
     float total = 0.f;
-    for (int gg = 0; gg < G; gg++) total += part[s * GT + rl * G + gg];
+    const int cs = cslot[s];
+    if (cs >= 0)
+      for (int gg = 0; gg < G; gg++) total += part[cs * GT + rl * G + gg];
     I3 d = mk(s % 5 - 2, (s / 5) % 5 - 2, s / 25 - 2);
     int J = m.wrap(l + 1, addI(m.coord(l + 1, row), d));
     bool canonical = J >= row && eqI(m.delta(l + 1, row, J), d) && m.active<T>(l + 1, row);
@@ -902,7 +911,7 @@ __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int 
     lin_s = lin;
   }
   int i = blockIdx.x * NTB + threadIdx.x;
-  if (l >= 1 && op != 3) {  // sweeps, residual, prolongation: active rows only
+  if (l >= 1 && op != 3 && op != 5) {  // sweeps, residual, prolongation: active rows only
     if (i >= (int)D.mg_rowcount[l]) return;
     i = D.mg_rowlist[D.lv[l].off + i];
   } else if (i >= D.lv[l].count)
@@ -914,6 +923,16 @@ __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int 
     case 2: residual_update<T>(m, l, i, m.apply<T>(l, a, i, lin_s)); break;
     case 3: restrict_cell<T>(m, l, i); break;
     case 4: prolong_cell<T>(m, l, a, b, i); break;
+    case 5:
+      // restriction into level l fused with the level's first pre-smoothing sweep, which starts
+      // from a zero iterate and so needs only the row's own b and scale (Chebyshev k = 1 into
+      // field 2, or the Jacobi sweep s b); the skipped inactive rows keep the restriction's zeros
+      restrict_cell<T>(m, l, i);
+      if (m.active<T>(l, i)) {
+        if (D.mg_smoother == 1) cheb_update<T>(m, l, 1, 1, i, true, 0.f);
+        else jacobi_update<T>(m, l, 1, 1, i, 0.f);
+      }
+      break;
   }
 }
 
@@ -1258,14 +1277,14 @@ template <class T> struct Cycle {
         else if (D.mg_rows_rr == 16) pdl_launch((k_mgl_rows<T, 16>), rows_grid(l, 16), NT, 0, s, D, phase, op, l, a, b, c);
         else if (D.mg_rows_rr == 64) pdl_launch((k_mgl_rows<T, 64>), rows_grid(l, 64), NT, 0, s, D, phase, op, l, a, b, c);
         else pdl_launch((k_mgl_rows<T, RR>), rows_grid(l, RR), NT, 0, s, D, phase, op, l, a, b, c);
-      });
+      }, l);
     else
       probed(kProbeRowThread, s, bytes, [&] {
         if (D.mg_thread_nt == 128)
           pdl_launch((k_mgl<T, 128>), (unsigned)((D.lv[l].count + 127) / 128), 128, 0, s, D, phase, op, l, a, b, c);
         else
           pdl_launch((k_mgl<T, NT>), grid_for(D.lv[l].count), NT, 0, s, D, phase, op, l, a, b, c);
-      });
+      }, l);
   }
   dim3 grid0() const { return dim3((unsigned)((D.nx + kTileX - 1) / kTileX), (unsigned)((D.ny + kTileY - 1) / kTileY), (unsigned)D.nz); }
   int smooth(int l, int field, bool zero, bool last0) {
@@ -1273,7 +1292,7 @@ template <class T> struct Cycle {
     for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
       bool first = zero && sweep == 0;
       bool fin = last0 && sweep == D.mg_smoothing - 1;
-      if (l == 0 && first && fused_first) {
+      if (first && (l == 0 ? fused_first != 0 : restrict_fused(l))) {
         field = 3 - field;
         continue;
       }
@@ -1291,6 +1310,11 @@ template <class T> struct Cycle {
       field = 3 - field;
     }
     return field;
+  }
+  // A level >= 1 reached through the regular per-level path has its first pre-smoothing sweep
+  // done by the launch that restricts into it (k_mgl op 5).
+  bool restrict_fused(int l) const {
+    return l >= 1 && l != D.L - 1 && l != D.mg_bottom && !(D.mg_coarse_from > 0 && l == D.mg_coarse_from && l < D.mg_bottom);
   }
   // pre- and post-smoothing flip the field mg_smoothing times each: a level ends in field 1
   int bottom_field() const { return 1; }
@@ -1317,7 +1341,7 @@ template <class T> struct Cycle {
     int field = smooth(l, 1, true, false);
     if (l == 0) pdl_launch((k_mg0_residual<T>), grid0(), NT, 0, s, D, phase, field);
     else level_op(l, 2, field, 0, 0);
-    pdl_launch((k_mgl<T>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, 3, l + 1, 0, 0, 0);
+    pdl_launch((k_mgl<T>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, restrict_fused(l + 1) ? 5 : 3, l + 1, 0, 0, 0);
     int cf = level(l + 1);
     pdl_launch((k_mgl<T>), gr, NT, 0, s, D, phase, 4, l, field, cf, 0);
     return smooth(l, field, false, l == 0 && D.mg_smoother == 1);
@@ -1385,7 +1409,8 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
     (void)lo;
     int G = ext[1] * ext[2], rpb = GT / G;
     unsigned gr = (unsigned)((D.lv[l].count + rpb - 1) / rpb);
-    pdl_launch((k_mg_galerkin<T>), gr, GT, 125 * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
+    const int slots = D.lv[l].gal_slots > 0 ? D.lv[l].gal_slots : 125;
+    pdl_launch((k_mg_galerkin<T>), gr, GT, (size_t)slots * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
     pdl_launch((k_mg_scale<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   }
   for (int l = 1; l < D.L; l++) pdl_launch((k_mg_ell<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);

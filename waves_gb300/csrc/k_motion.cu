@@ -372,9 +372,22 @@ struct Mac {
   // donor lookups reduce to two loads each; the arithmetic is unchanged.
   // With want_value false only `valid` is produced (the value and limits are not needed): the
   // fast path then skips the eight value loads.
-  DI float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1, bool want_value = true) const {
+  // A sample point in units of the cell size, x / h per axis: the lattice coordinates of every
+  // component and the solid test of the point start from the same three quotients, so a point's
+  // three samples and its solid test divide once.
+  DI F3 scaled(F3 x) const { return mf(x.x / m.D.hx, x.y / m.D.hy, x.z / m.D.hz); }
+  template <bool FAST = false>
+  DI float sample(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1, bool want_value = true,
+                  bool* fail = nullptr) const {
+    return sample_s<FAST>(scaled(x), axis, forward, valid, lim0, lim1, want_value, fail);
+  }
+  // FAST: only the fast path is compiled in; where its precondition fails, `fail` is set and the
+  // result is left undefined (the caller hands the face to the general kernel).
+  template <bool FAST = false>
+  DI float sample_s(F3 xs, int axis, bool forward, bool& valid, float& lim0, float& lim1, bool want_value = true,
+                    bool* fail = nullptr) const {
     const Dev& D = m.D;
-    F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);
+    F3 lattice = mf(xs.x - .5f, xs.y - .5f, xs.z - .5f);
     lattice[axis] += .5f;
     I3 lo = mk((int)floorf(lattice.x), (int)floorf(lattice.y), (int)floorf(lattice.z));
     if ((D.flags & 8) == 0 && !D.px && lo.x >= 0 && lo.y >= 0 && lo.x + 1 < D.nx + (axis == 0) &&
@@ -384,15 +397,18 @@ struct Mac {
       lim0 = 1e20f;
       lim1 = -1e20f;
       valid = true;
+      // face indices of the 2 x 2 x 2 donors: rows (y, z) of the block, z wrapped (a face at
+      // z = nz is the canonical z = 0); every index fits 32 bits
       const int mx_ = D.nx + (axis == 0), my_ = D.ny + (axis == 1);
-      const long long base = axis == 0 ? 0 : (axis == 1 ? D.NU : D.NU + D.NV);
+      const int base = axis == 0 ? 0 : (axis == 1 ? (int)D.NU : (int)(D.NU + D.NV));
+      const int qz0 = pidx(lo.z, D.nz), qz1 = qz0 + 1 == D.nz ? 0 : qz0 + 1;
+      const int r00 = base + lo.x + mx_ * (lo.y + my_ * qz0), r01 = base + lo.x + mx_ * (lo.y + my_ * qz1);
       const float* src = forward ? D.fwd : m.A + D.N;
       float values[8];
 #pragma unroll
       for (int c = 0; c < 8; c++) {
         int xx = c & 1, y = (c >> 1) & 1, z = c >> 2;
-        int qz = pidx(lo.z + z, D.nz);  // wrap; a face at z = nz is the canonical z = 0
-        long long f = base + (long long)(lo.x + xx) + (long long)mx_ * ((long long)(lo.y + y) + (long long)my_ * qz);
+        const int f = (z ? r01 : r00) + y * mx_ + xx;
         bool supported = vb[f] > .5f;
         float value = want_value ? src[f] : 0.f;
         values[c] = value;
@@ -408,12 +424,19 @@ struct Mac {
       float lower = __fmaf_rn(t.y, b - a, a), upper = __fmaf_rn(t.y, e - d, d);
       return __fmaf_rn(t.z, upper - lower, lower);
     }
-    return sample_slow(x, axis, forward, valid, lim0, lim1);
+    if constexpr (FAST) {
+      *fail = true;
+      valid = false;
+      lim0 = lim1 = 0.f;
+      return 0.f;
+    } else {
+      return sample_slow(xs, axis, forward, valid, lim0, lim1);
+    }
   }
-  __device__ __noinline__ float sample_slow(F3 x, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
+  __device__ __noinline__ float sample_slow(F3 xs, int axis, bool forward, bool& valid, float& lim0, float& lim1) const {
     const Grid& g = m.g;
     const Dev& D = m.D;
-    F3 lattice = mf(x.x / D.hx - .5f, x.y / D.hy - .5f, x.z / D.hz - .5f);
+    F3 lattice = mf(xs.x - .5f, xs.y - .5f, xs.z - .5f);
     lattice[axis] += .5f;
     I3 lo = mk((int)floorf(lattice.x), (int)floorf(lattice.y), (int)floorf(lattice.z));
     F3 t = mf(fract_(lattice.x), fract_(lattice.y), fract_(lattice.z));
@@ -455,10 +478,8 @@ struct Mac {
     for (int axis = 0; axis < 3; axis++) v[axis] = sample(x, axis, false, valid, l0, l1v);
     return v;
   }
-  DI bool solid_at(F3 p) const {
-    const Dev& D = m.D;
-    return m.g.solid(mk((int)floorf(p.x / D.hx), (int)floorf(p.y / D.hy), (int)floorf(p.z / D.hz)));
-  }
+  DI bool solid_at(F3 p) const { return solid_at_s(scaled(p)); }
+  DI bool solid_at_s(F3 ps) const { return m.g.solid(mk((int)floorf(ps.x), (int)floorf(ps.y), (int)floorf(ps.z))); }
   DI F3 trace(F3 x, float d) const {
     F3 s = velocity(x);
     float hd = .5f * d;
@@ -496,21 +517,24 @@ DI F3 face_x(const Dev& D, const Grid& g, I3 q, int axis) {
 // cached_advection, forward pass (coupled_motion.glslinc:170-179); dbg (optional) gets 16 floats.
 // The nine samples (three components at x, at the midpoint and at the end point) come from one
 // sampler call site in a loop that is not unrolled, so the sampler is emitted once per kernel.
-DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float* dbg) {
+template <bool FAST = false>
+DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float* dbg, bool* fail = nullptr) {
   const Dev& D = mc.m.D;
   const long long nf = D.NF;
   const float hd = .5f * d;
   F3 p = x, sv = mf(0.f, 0.f, 0.f), mid = x, end = x;
+  F3 ps[3];  // the three points in units of the cell size
   float value = 0.f, l0 = 0.f, l1v = 0.f;
   unsigned ok = 7u;  // bit s: every sample of stage s supported
 #pragma unroll 1
   for (int stage = 0; stage < 3; stage++) {
     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    ps[stage] = mc.scaled(p);
 #pragma unroll 1
     for (int a = 0; a < 3; a++) {
       bool valid;
       float lo, hi;
-      const float s = mc.sample(p, a, false, valid, lo, hi, stage < 2 || a == axis);
+      const float s = mc.template sample_s<FAST>(ps[stage], a, false, valid, lo, hi, stage < 2 || a == axis, fail);
       if (!valid) ok &= ~(1u << stage);
       if (a == 0) v0 = s;
       else if (a == 1) v1 = s;
@@ -530,8 +554,11 @@ DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float*
       p = end;
     }
   }
+  if constexpr (FAST) {
+    if (*fail) return 0.f;  // nothing written: the general kernel takes the face
+  }
   const bool vs = ok & 1u, vm = ok & 2u, ve = ok & 4u;
-  bool clear = !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end);
+  bool clear = !mc.solid_at_s(ps[0]) && !mc.solid_at_s(ps[1]) && !mc.solid_at_s(ps[2]);
   if (dbg) {
     float t[16] = {x.x, x.y, x.z, sv.x, sv.y, sv.z, (float)vs, mid.x, mid.y, mid.z, (float)vm, end.x, end.y, end.z, (float)ve, (float)clear};
     for (int k = 0; k < 16; k++) dbg[k] = t[k];
@@ -547,7 +574,8 @@ DI float mac_forward(const Mac& mc, F3 x, int axis, float d, long long i, float*
 }
 // cached_advection, corrected pass (coupled_motion.glslinc:180-187): the reverse trace from the
 // cached start velocity, six samples from one call site.
-DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
+template <bool FAST = false>
+DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i, bool* fail = nullptr) {
   const Dev& D = mc.m.D;
   const long long nf = D.NF;
   const float forward = D.fwd[i];
@@ -557,16 +585,18 @@ DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
   const float hd = .5f * rd;
   const F3 mid = mf(x.x - hd * sv.x, x.y - hd * sv.y, x.z - hd * sv.z);
   F3 p = mid, end = mid;
+  F3 ps[2];  // mid and end in units of the cell size
   float backward = 0.f;
   bool ok = true;
 #pragma unroll 1
   for (int stage = 0; stage < 2; stage++) {
     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    ps[stage] = mc.scaled(p);
 #pragma unroll 1
     for (int a = 0; a < 3; a++) {
       bool valid;
       float lo, hi;
-      const float s = mc.sample(p, a, stage == 1 && a == axis, valid, lo, hi, stage == 0 || a == axis);
+      const float s = mc.template sample_s<FAST>(ps[stage], a, stage == 1 && a == axis, valid, lo, hi, stage == 0 || a == axis, fail);
       ok = ok && valid;
       if (a == 0) v0 = s;
       else if (a == 1) v1 = s;
@@ -579,7 +609,10 @@ DI float mac_correct(const Mac& mc, F3 x, int axis, float d, long long i) {
     }
   }
   float corrected = forward + .5f * (mc.m.A[D.N + i] - backward);
-  return (ok && !mc.solid_at(x) && !mc.solid_at(mid) && !mc.solid_at(end) && corrected >= D.tcache[i] &&
+  if constexpr (FAST) {
+    if (*fail) return 0.f;
+  }
+  return (ok && !mc.solid_at(x) && !mc.solid_at_s(ps[0]) && !mc.solid_at_s(ps[1]) && corrected >= D.tcache[i] &&
           corrected <= D.tcache[nf + i])
              ? corrected
              : forward;
@@ -620,7 +653,7 @@ template <int op, bool cached> DI void mac_face(const Dev& D, const Motion& m, c
 // (zero) here.  mac_ctr: [0] interior count, [1] boundary count, [2]/[3] op 27/28 work cursors.
 __global__ void k_mac_reset(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
-  if (threadIdx.x < 4) D.mac_ctr[threadIdx.x] = 0u;
+  if (threadIdx.x < kMacCounters) D.mac_ctr[threadIdx.x] = 0u;
 }
 __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
@@ -656,12 +689,16 @@ __global__ void __launch_bounds__(NT) k_mac_list(const __grid_constant__ Dev D) 
   }
 }
 // Persistent pass over the work list: each warp takes 32 consecutive entries at a time, boundary
-// faces first, so a slow warp never holds idle lanes of a finished block.
+// faces first, so a slow warp never holds idle lanes of a finished block.  With `split`, the
+// interior faces were taken by k_mac_fast and this pass covers the boundary faces and the faces
+// k_mac_fast handed over (mac_ovf).
 template <int op, bool cached, int MINB = 2>
-__global__ void __launch_bounds__(NT, MINB) k_mac(const __grid_constant__ Dev D) {
+__global__ void __launch_bounds__(NT, MINB) k_mac(const __grid_constant__ Dev D, int split) {
   grid_dep_wait(D.pdl_early);
   if (!setup_on(D)) return;
-  const unsigned n_int = D.mac_ctr[0], n_edge = D.mac_ctr[1], total = n_int + n_edge;
+  const unsigned n_edge = D.mac_ctr[1];
+  const unsigned n_rest = split ? D.mac_ctr[op == 27 ? 6 : 7] : D.mac_ctr[0];
+  const unsigned total = n_edge + n_rest;
   unsigned* cursor = D.mac_ctr + (op == 27 ? 2 : 3);
   const int lane = threadIdx.x & 31;
   while (true) {
@@ -672,10 +709,49 @@ __global__ void __launch_bounds__(NT, MINB) k_mac(const __grid_constant__ Dev D)
     if (base >= total) break;
     const unsigned k = base + lane;
     if (k < total) {
-      const long long i = k < n_edge ? (long long)D.mac_list[D.NF - 1 - (long long)k] : (long long)D.mac_list[k - n_edge];
+      const long long i = k < n_edge ? (long long)D.mac_list[D.NF - 1 - (long long)k]
+                                     : (long long)(split ? D.mac_ovf[k - n_edge] : D.mac_list[k - n_edge]);
       Motion m(D);  // views of the parameter block, rebuilt per face so none of it stays live
       Mac mc(m);
       mac_face<op, cached>(D, m, mc, i);
+    }
+  }
+}
+// The interior faces of the work list (no solid cell or domain edge within three cells, so every
+// donor of every trace is a plain stored face) with the sampler's fast path alone: no boundary
+// code in the kernel, so fewer registers and more resident warps.  A face whose trace leaves the
+// fast path's region is handed over to the general pass untouched.
+template <int op>
+__global__ void __launch_bounds__(NT, 4) k_mac_fast(const __grid_constant__ Dev D) {
+  grid_dep_wait(D.pdl_early);
+  if (!setup_on(D)) return;
+  const unsigned total = D.mac_ctr[0];
+  unsigned* cursor = D.mac_ctr + (op == 27 ? 4 : 5);
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    __syncwarp();
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(cursor, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const unsigned k = base + lane;
+    if (k < total) {
+      const long long i = (long long)D.mac_list[k];
+      Motion m(D);
+      Mac mc(m);
+      I3 q;
+      int axis;
+      m.g.unpack_face(i, q, axis);
+      const F3 x = face_x(D, m.g, q, axis);
+      bool fail = false;
+      if constexpr (op == 27) {
+        const float value = mac_forward<true>(mc, x, axis, m.dt, i, nullptr, &fail);
+        if (!fail) D.fwd[i] = value;
+      } else {
+        const float value = mac_correct<true>(mc, x, axis, m.dt, i, &fail);
+        if (!fail) m.Cb[D.N + i] = value;
+      }
+      if (fail) D.mac_ovf[atomicAdd(D.mac_ctr + (op == 27 ? 6 : 7), 1u)] = (int)i;
     }
   }
 }
@@ -764,17 +840,29 @@ void launch_maccormack(const Dev& D, cudaStream_t s) {
   // cache, its six fields); op 28 reads those, the faces and the band, and writes the candidate.
   const double nf = (double)D.NF, cache = (D.flags & 4) ? 6.0 : 0.0;
   if (D.flags & 4) {
-    if (D.mac_minb == 3) {
-      probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true, 3>), D.mac_grid, NT, 0, s, D); });
-      probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true, 3>), D.mac_grid, NT, 0, s, D); });
-    } else {
-      probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true>), D.mac_grid2, NT, 0, s, D); });
-      probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true>), D.mac_grid2, NT, 0, s, D); });
-    }
+    // interior faces on the fast-path kernel, then boundary and handed-over faces
+    const int split = D.mac_split ? 1 : 0;
+    if (split) probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac_fast<27>), D.mac_fast_grid, NT, 0, s, D); });
+    if (D.mac_minb == 3)
+      probed(kProbeMac, s, split ? 0.0 : 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true, 3>), D.mac_grid, NT, 0, s, D, split); });
+    else
+      probed(kProbeMac, s, split ? 0.0 : 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, true>), D.mac_grid2, NT, 0, s, D, split); });
+    if (split) probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac_fast<28>), D.mac_fast_grid, NT, 0, s, D); });
+    if (D.mac_minb == 3)
+      probed(kProbeMac, s, split ? 0.0 : 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true, 3>), D.mac_grid, NT, 0, s, D, split); });
+    else
+      probed(kProbeMac, s, split ? 0.0 : 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, true>), D.mac_grid2, NT, 0, s, D, split); });
   } else {
-    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, false>), D.mac_grid, NT, 0, s, D); });
-    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, false>), D.mac_grid, NT, 0, s, D); });
+    probed(kProbeMac, s, 4.0 * nf * (3.0 + cache), [&] { pdl_launch((k_mac<27, false>), D.mac_grid, NT, 0, s, D, 0); });
+    probed(kProbeMac, s, 4.0 * nf * (4.0 + cache), [&] { pdl_launch((k_mac<28, false>), D.mac_grid, NT, 0, s, D, 0); });
   }
+}
+int mac_fast_blocks() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mac_fast<28>, NT, 0) != cudaSuccess)
+    return 0;
+  return sms * (per_sm > 0 ? per_sm : 1);
 }
 
 }  // namespace wg

@@ -282,5 +282,7 @@ __global__ void k_delay(long long cycles) {
   }
 }
 void launch_delay(cudaStream_t s, long long cycles) { k_delay<<<1, 1, 0, s>>>(cycles); }
+__global__ void k_empty() {}
+void launch_empty(cudaStream_t s) { k_empty<<<1, 1, 0, s>>>(); }
 
 }  // namespace wg

@@ -21,21 +21,26 @@ enum ProbeKind {
   kProbeRowThread = 3,  // k_mgl ops 0-2, level >= 1 sweeps with one thread per row
   kProbeSweepVof = 4,   // k_sweep_update, VOF flux + update of one direction
   kProbeAll = 5,        // every kernel of the trial (bytes not counted)
-  kProbeCount = 6
+  kProbeEmpty = 6,      // calibration: an empty kernel bracketed as a probed launch is (kind + all)
+  kProbeEmptyInner = 7, // the inner bracket of that calibration
+  kProbeCount = 8
 };
+// `level` >= 1 marks a multigrid level sweep whose bytes were counted over all rows of the level;
+// the probe scales them to the rows the sweep visits (the active rows) once the trial has run.
 struct ProbeRec {
   int kind;
   cudaEvent_t a, b;
   double bytes;
+  int level;
 };
 extern thread_local std::vector<ProbeRec>* g_probe;
-template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launch) {
+template <class F> void probed(int kind, cudaStream_t s, double bytes, F&& launch, int level = -1) {
   std::vector<ProbeRec>* p = g_probe;
   if (!p) {
     launch();
     return;
   }
-  ProbeRec r{kind, nullptr, nullptr, bytes};
+  ProbeRec r{kind, nullptr, nullptr, bytes, level};
   cudaEventCreate(&r.a);
   cudaEventCreate(&r.b);
   cudaEventRecord(r.a, s);
@@ -73,17 +78,21 @@ void launch_cg_init(const Dev& D, cudaStream_t s);
 void launch_warm_start(const Dev& D, cudaStream_t s);  // learned warm start after op 2 (no-op when not configured)
 // k_net.cu
 void launch_warm_network(const Dev& D, cudaStream_t s);
+void setup_warm_network();  // shared-memory limits of the tcgen05 layers
 void launch_cg_matvec(const Dev& D, cudaStream_t s);
 void launch_cg_update(const Dev& D, cudaStream_t s);
 void launch_cg_direction(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int use_handle);
 void launch_set_cond(const Dev& D, cudaStream_t s, cudaGraphConditionalHandle h, int which);
 void launch_delay(cudaStream_t s, long long cycles);
+void launch_empty(cudaStream_t s);  // one empty one-thread kernel (probe calibration)
 // k_motion.cu
 void launch_motion_cfl(const Dev& D, cudaStream_t s);
 void launch_sweep(const Dev& D, cudaStream_t s);
 void launch_maccormack(const Dev& D, cudaStream_t s);
 int mac_blocks();   // resident blocks of the persistent MacCormack kernel (3 per SM form)
 int mac_blocks2();  // the same for the 2-per-SM form
+int mac_fast_blocks();  // resident blocks of the interior fast-path MacCormack pass
+constexpr int kMacCounters = 8;
 void launch_debug_sample(const Dev& D, cudaStream_t s, const float* x, int axis, int forward, float* out);
 // k_geom.cu
 void launch_coastal(const Dev& D, cudaStream_t s);

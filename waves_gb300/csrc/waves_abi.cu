@@ -375,6 +375,11 @@ waves_status setup_device(waves_handle* h) {
   if (k.warm_start) {
     D.net_on = 1;
     AL(D.net_w, (size_t)WAVES_NET_LAYERS * wg::kNetLayerWords, false, "net_weights");
+    AL(D.net_wt, (size_t)WAVES_NET_LAYERS * 27 * 256, false, "net_weights_tcgen05");
+    // the layers on tcgen05 unless WAVES_NET_MMA=sync asks for the warp-level mma.sync form
+    D.net_tc05 = 1;
+    if (const char* e = getenv("WAVES_NET_MMA")) D.net_tc05 = std::strcmp(e, "sync") != 0;
+    wg::setup_warm_network();
     AL(D.net_b, (size_t)WAVES_NET_LAYERS * 16, false, "net_bias");
     AL(D.net_scale, 4, false, "net_scale");
     AL(D.net_act, (size_t)2 * N * 16, false, "net_activations");
@@ -382,8 +387,15 @@ waves_status setup_device(waves_handle* h) {
   }
   AL(D.ext_nb, NF, false, "ext_neighbours");
   AL(D.mac_list, NF, false, "mac_list");
-  AL(D.mac_ctr, 4, false, "mac_counters");
+  AL(D.mac_ctr, wg::kMacCounters, false, "mac_counters");
+  AL(D.mac_ovf, NF, false, "mac_handover");
   D.mac_grid = wg::mac_blocks();
+  D.mac_fast_grid = wg::mac_fast_blocks();
+  if (D.mac_fast_grid <= 0) D.mac_fast_grid = 4 * 152;
+  // interior faces on the fast-path pass where the fast path exists (not periodic in x, the
+  // interior fast path of flag 8 off); WAVES_MAC_SPLIT=0 runs every face on the general pass
+  D.mac_split = (!D.px && (D.flags & 8) == 0) ? 1 : 0;
+  if (const char* e = getenv("WAVES_MAC_SPLIT")) D.mac_split = D.mac_split && atoi(e) != 0;
   D.pdl_early = 0;
   if (const char* e = getenv("WAVES_PDL")) D.pdl_early = atoi(e) == 2;
   if (D.mac_grid <= 0) D.mac_grid = 2 * 152;
@@ -449,6 +461,51 @@ waves_status setup_device(waves_handle* h) {
     AL(dlin, lin.size(), false, "stencil_linear");
     CK(cudaMemcpyAsync(dlin, lin.data(), lin.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     D.stencil_lin = dlin;
+    // Galerkin partials per stencil entry for the coarse levels with small stencils.  A product
+    // term's offset d is a difference of two transfer targets; the transfers clamp at the bottom
+    // and the sides (moving d one step toward zero on that axis) and fold short periodic axes to
+    // the minimum image, so the stencil must be closed under both for every term to find its slot.
+    std::vector<signed char> cslot((size_t)wg::kMaxLevels * 125, -1);
+    for (int l = 1; l < D.L; l++) {
+      wg::MGLevelDev& lv = D.lv[l];
+      lv.gal_slots = 0;
+      const int S = lv.stencil;
+      if (S > 48) continue;
+      const int* st = &h->stencil_tab[3 * lv.soff];
+      const int n[3] = {lv.nx, lv.ny, lv.nz};
+      auto find = [&](int x, int y, int z) {
+        for (int k = 0; k < S; k++)
+          if (st[3 * k] == x && st[3 * k + 1] == y && st[3 * k + 2] == z) return k;
+        return -1;
+      };
+      bool closed = true;
+      for (int k = 0; k < S && closed; k++)
+        for (int a = 0; a < 3 && closed; a++) {
+          int d[3] = {st[3 * k], st[3 * k + 1], st[3 * k + 2]};
+          const bool periodic = a == 2 || (a == 0 && D.px);
+          if (periodic) {
+            const int m = n[a];
+            d[a] = ((d[a] + m / 2) % m + m) % m - m / 2;
+          } else if (d[a] != 0) {
+            d[a] -= d[a] > 0 ? 1 : -1;
+          }
+          closed = find(d[0], d[1], d[2]) >= 0;
+        }
+      if (!closed) continue;
+      lv.gal_slots = S;
+      for (int k = 0; k < S; k++) {
+        const int* o = &st[3 * k];
+        if (o[0] < -2 || o[0] > 2 || o[1] < -2 || o[1] > 2 || o[2] < -2 || o[2] > 2) {
+          lv.gal_slots = 0;
+          break;
+        }
+        cslot[(size_t)l * 125 + (o[0] + 2) + 5 * ((o[1] + 2) + 5 * (o[2] + 2))] = (signed char)k;
+      }
+    }
+    signed char* dcs;
+    AL(dcs, cslot.size(), false, "galerkin_slots");
+    CK(cudaMemcpyAsync(dcs, cslot.data(), cslot.size(), cudaMemcpyHostToDevice, h->stream));
+    D.gal_cslot = dcs;
     CK(cudaStreamSynchronize(h->stream));
   }
   // Restriction tables (pressure_multigrid.glslinc:208-221): for coarse level l, axis a, coarse
@@ -1483,6 +1540,7 @@ waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model*
   // (first register) and 2t + 8, 2t + 9 (second), low half first; absent channels are zero.
   std::vector<uint32_t> frag((size_t)WAVES_NET_LAYERS * wg::kNetLayerWords, 0u);
   std::vector<float> bias((size_t)WAVES_NET_LAYERS * 16, 0.f);
+  std::vector<uint16_t> wt((size_t)WAVES_NET_LAYERS * 27 * 256, 0);
   for (int l = 0; l < WAVES_NET_LAYERS; l++) {
     const int CI = ci_of[l], CO = co_of[l], tiles = CO > 8 ? 2 : 1;
     auto w = [&](int co, int tap, int ci) -> uint32_t {
@@ -1498,9 +1556,17 @@ waves_status waves_set_warm_start(waves_handle* h, const waves_warm_start_model*
           frag[at + 1] = w(n, tap, 2 * t + 8) | (w(n, tap, 2 * t + 9) << 16);
         }
     for (int co = 0; co < CO; co++) bias[(size_t)l * 16 + co] = model->bias[l][co];
+    // tcgen05 B operand, K-major without swizzle: per tap two planes (input channels 0-7, 8-15),
+    // each one 16-byte row of 8 channels per output channel
+    for (int tap = 0; tap < 27; tap++)
+      for (int half = 0; half < 2; half++)
+        for (int n = 0; n < 16; n++)
+          for (int k = 0; k < 8; k++)
+            wt[(size_t)l * 27 * 256 + (size_t)tap * 256 + half * 128 + n * 8 + k] = (uint16_t)w(n, tap, half * 8 + k);
   }
   const float scale[4] = {model->input_scale[0], model->input_scale[1], model->input_scale[2], model->output_scale};
   CK(cudaMemcpyAsync(D.net_w, frag.data(), frag.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(D.net_wt, wt.data(), wt.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(D.net_b, bias.data(), bias.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(D.net_scale, scale, sizeof(scale), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(D.c + wg::kNetLoaded, &on, sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1555,9 +1621,22 @@ waves_status waves_debug_probe_trial(waves_handle* h, waves_kernel_probe* out, i
   int32_t done = 0;
   // one host-scheduled trial with every CG iteration checked: no probed launch is a no-op
   if ((st = upload_quota(h)) == WAVES_OK) st = host_trial(h, 1);
+  // calibration: the cost of the two nested event brackets of a probed launch, measured on an
+  // empty kernel bracketed the same way (kind kProbeEmpty around kProbeEmptyInner)
+  if (st == WAVES_OK)
+    for (int k = 0; k < 64; k++)
+      wg::probed(wg::kProbeEmpty, h->stream, 0.0, [&] { wg::probed(wg::kProbeEmptyInner, h->stream, 0.0, [&] { wg::launch_empty(h->stream); }); });
   wg::g_probe = nullptr;
   if (st == WAVES_OK) done = 1;
   if (st == WAVES_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) st = WAVES_CUDA_ERROR;
+  // the level sweeps visit the active rows only: their bytes, counted over every row, are scaled
+  // to the active rows of the trial's hierarchy
+  unsigned active[wg::kMaxLevels] = {0};
+  if (st == WAVES_OK && cudaMemcpy(active, h->D.mg_rowcount, sizeof(active), cudaMemcpyDeviceToHost) != cudaSuccess)
+    st = WAVES_CUDA_ERROR;
+  for (wg::ProbeRec& r : recs)
+    if (r.level >= 1 && r.level < h->D.L && h->D.lv[r.level].count > 0)
+      r.bytes *= (double)active[r.level] / (double)h->D.lv[r.level].count;
   for (const wg::ProbeRec& r : recs) {
     float ms = 0.f;
     if (st == WAVES_OK && r.kind < capacity && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
