@@ -30,7 +30,8 @@ waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size
  * sweeps (one thread per row), 4 VOF flux + update, 5 every kernel of the trial (launches and
  * time only), 6 and 7 the calibration after the trial: 64 launches of an empty kernel bracketed
  * the way a probed launch is (6 the outer, 7 the inner event pair), whose time per launch is the
- * cost the brackets add to each probed launch.  The trial advances the simulation like any
+ * cost the brackets add to each probed launch, 8 the coarse leg of the V-cycle in one cluster
+ * launch (bytes of its level sweeps).  The trial advances the simulation like any
  * other; *trials is 0 when no trial was active (quota met). */
 typedef struct waves_kernel_probe {
   int32_t kind;

@@ -26,6 +26,7 @@ template <class R> struct MG {
   std::vector<Level> levels;
   std::vector<std::vector<R>> v;              // 8 fields x count per level
   std::vector<std::vector<R>> matrix;         // canonical 125-slot rows (l >= 1)
+  std::vector<R> ap;                          // A P of the Galerkin product's first stage (125 per fine row)
   std::vector<std::vector<R>> ellv;           // ELL values [k][i] (l >= 1)
   std::vector<std::vector<int>> ellc;         // ELL columns [k][i]
   std::vector<std::vector<int>> tid;          // transfer cache ids [k][i] (l < L-1)

@@ -36,6 +36,12 @@ def tank_jacobi(**kw):
     return tank_small(mg_smoother=0, mg_smoothing=2, mg_maintenance=0, **kw)
 
 
+def beach_coarse_jacobi(**kw):
+    """The coarse beach with Jacobi smoothing (two sweeps) and rebuild-every-trial maintenance: the
+    Jacobi path on a five-level plan (two levels between the finest and a shared-memory bottom)."""
+    return beach_coarse(mg_smoother=0, mg_smoothing=2, mg_maintenance=0, **kw)
+
+
 def tank_periodic(**kw):
     """The small tank, periodic in x (the periodic-x index, delta and transfer paths)."""
     return tank_small(periodic_x=1, **kw)
@@ -116,7 +122,8 @@ def aggr3(**kw):
 
 
 CASES = {"tank_small": tank_small, "tank_ref_cfl": tank_ref_cfl, "beach_coarse": beach_coarse,
-         "beach_slope": beach_slope, "beach_slope_bf16": beach_slope_bf16, "tank_bf16": tank_bf16,
+         "beach_slope": beach_slope, "beach_coarse_jacobi": beach_coarse_jacobi, "beach_slope_bf16": beach_slope_bf16,
+         "tank_bf16": tank_bf16,
          "tank_jacobi": tank_jacobi, "tank_periodic": tank_periodic, "dam_break": dam_break, "jets": jets,
          "wave_periodic": wave_periodic, "box_pool": box_pool, "inflow": inflow, "absorber": absorber,
          "height_normals": height_normals, "linear_air": linear_air, "max_face_cfl": max_face_cfl,

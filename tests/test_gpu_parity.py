@@ -72,15 +72,34 @@ def test_step_parity(gpu_lib, name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["beach_slope", "beach_slope_bf16"])
-@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1", "WAVES_MG_COARSE=1"])
+@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1", "WAVES_MG_COARSE=1",
+                                     "WAVES_MG_LEG=1"])
 def test_step_parity_kernel_variants(gpu_lib, name, variant, monkeypatch):
     """Kernel forms that the small grids above do not reach: the level >= 1 sweeps with one
     thread per row (large levels use it; small ones use the product-parallel rows), the bottom
-    levels solved from global memory (used when they do not fit the shared-memory stage), and the
-    coarse levels as one cooperative launch instead of level by level."""
+    levels solved from global memory (used when they do not fit the shared-memory stage), the
+    coarse levels as one cooperative launch, and the coarse leg as one thread-block cluster
+    launch, instead of level by level."""
     key, value = variant.split("=")
     monkeypatch.setenv(key, value)
     cfg = CASES[name]()
+    g = wg.WavesSolver(cfg)
+    o = Oracle(cfg, 32)
+    for step in range(1, 4):
+        g.request_steps(step)
+        g.run()
+        o.request_steps(step)
+        o.run()
+        problems = compare_state(g, o, cfg, f"step {step}")
+        assert not problems, "\n".join(problems)
+
+
+@pytest.mark.gpu
+def test_step_parity_cluster_leg_jacobi(gpu_lib, monkeypatch):
+    """The one-cluster coarse leg with Jacobi smoothing, over two levels and the bottom (the
+    coarse beach), bit for bit against the oracle."""
+    monkeypatch.setenv("WAVES_MG_LEG", "1")
+    cfg = CASES["beach_coarse_jacobi"]()
     g = wg.WavesSolver(cfg)
     o = Oracle(cfg, 32)
     for step in range(1, 4):

@@ -145,6 +145,7 @@ struct Dev {
   void* mgv;                 // 8 fields x total_nodes (float or bf16): 0 rhs,1/2 x,3 active,4 scale,6 res,7 cheb d
   long long mg_nodes;        // total nodes over all levels
   float* mgmat;              // canonical 125-slot rows of levels >= 1 (FP32, build only)
+  float* gal_ap;             // A P of the Galerkin product from a fine level >= 1 (125 per fine cell)
   void* mgell;               // ELL values [k][i] of levels >= 1 (float or bf16)
   int* mgtid;                // transfer cache ids
   float* mgtw;               // transfer cache weights
@@ -170,6 +171,8 @@ struct Dev {
   int mg_coarse_from;        // first level of the one-launch coarse V-cycle (0: not used)
   int coarse_blocks;         // blocks of that cooperative launch (one per SM)
   unsigned* gbar;            // its grid barrier: arrival count, generation
+  int mg_leg_from;           // first level of the one-cluster coarse leg (0: not used)
+  int mg_leg_smem;           // dynamic shared memory of each block of that launch
 };
 
 // Reduction sites (one last-block counter each).

@@ -570,6 +570,143 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
     D.mgmat[cl.moff + (long long)row * 125 + s] = canonical ? total : 0.f;
   }
 }
+// Galerkin product from a fine level l >= 1 in two stages (the oracle's mg_galerkin_ap and
+// mg_galerkin_pt, the same additions in the same order).  Stage 1: one thread per active fine row
+// i (the level's active-row list) accumulates A P over the 125 coarse offsets e = delta(home(i), J)
+// (home(i) = the coarse cell containing i) in shared memory, in the order stencil neighbour j,
+// transfer of j; the block then writes its rows' 125 slots to gal_ap (row-major by fine cell).
+constexpr int GA = 64;  // stage-1 threads per block (125 x 64 x 4 B = 32 KB of partials)
+template <class T> __global__ void __launch_bounds__(GA) k_mg_gal_ap(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait(D.pdl_early);
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  extern __shared__ float acc[];  // [125][GA]
+  __shared__ I3 offs[kMaxStencil];
+  __shared__ int rows[GA];
+  const MG m(D);
+  const MGLevelDev& fl = D.lv[l];
+  const int t = threadIdx.x;
+  for (int k = t; k < fl.stencil; k += GA) offs[k] = m.offset(l, k);
+  const int nrows = (int)D.mg_rowcount[l];
+  const long long tstride = fl.count;
+  for (int r0 = blockIdx.x * GA; r0 < nrows; r0 += gridDim.x * GA) {  // uniform over the block
+    for (int e = 0; e < 125; e++) acc[e * GA + t] = 0.f;
+    const bool ok = r0 + t < nrows;
+    const int i = ok ? D.mg_rowlist[fl.off + r0 + t] : 0;
+    rows[t] = ok ? i : -1;
+    __syncthreads();
+    const I3 qi = m.coord(l, i);
+    const I3 home = mk(qi.x / fl.fx, qi.y / fl.fy, qi.z / fl.fz);
+    for (int k = 0; k < fl.stencil; k++) {
+      // every load of one neighbour (its activity, the coefficient, its transfers) is issued
+      // before the first test; a neighbour outside the grid loads from i instead
+      const I3 off = offs[k];
+      I3 qj = addI(qi, off);
+      const bool in = m.wrap_q(l, qj);
+      const int j = in ? qj.x + fl.nx * (qj.y + fl.ny * qj.z) : i;
+      if (!in) qj = qi;
+      const bool uniq = eqI(m.delta_q(l, qi, qj), off);
+      const bool ilo = i <= j;
+      const I3 d = ilo ? m.delta_q(l, qi, qj) : m.delta_q(l, qj, qi);
+      const long long maddr =
+          (abs(d.x) > 2 || abs(d.y) > 2 || abs(d.z) > 2) ? -1 : fl.moff + (long long)(ilo ? i : j) * 125 + MG::slot(d);
+      const bool actj = m.active<T>(l, j);
+      const float aij = maddr >= 0 ? D.mgmat[maddr] : 0.f;
+      const long long tj = fl.toff + j;
+      float wv[8];
+      unsigned long long qv[8];
+#pragma unroll
+      for (int b = 0; b < 8; b++)
+        if (b < fl.twidth) {
+          wv[b] = D.mgtw[tj + b * tstride];
+          qv[b] = D.mgtq[tj + b * tstride];
+        }
+      const bool use = ok && in && actj && uniq && aij != 0.f;
+#pragma unroll
+      for (int b = 0; b < 8; b++) {
+        if (b >= fl.twidth) break;
+        const bool ub = use && wv[b] > 0.f;
+        const I3 e = m.delta_q(l + 1, home, MG::unpack(qv[b]));
+        const bool far = abs(e.x) > 2 || abs(e.y) > 2 || abs(e.z) > 2;
+        if (ub && far) D.c[7] = 31;
+        if (ub && !far) acc[MG::slot(e) * GA + t] += aij * wv[b];
+      }
+    }
+    __syncthreads();
+    // the block's rows, 125 consecutive floats each
+    for (int u = t; u < GA * 125; u += GA) {
+      const int r = u / 125, e = u - r * 125;
+      if (rows[r] >= 0) D.gal_ap[(long long)rows[r] * 125 + e] = acc[e * GA + r];
+    }
+    __syncthreads();
+  }
+}
+// Stage 2: one block per coarse row I.  The children of I (the box of child_range, in the order
+// gz, gy, gx) with their home cells and their transfer weights to I go to shared memory; thread s
+// (a slot, d_s = the 5 x 5 x 5 offset) then adds, for a canonical slot (J = I + d_s, J >= I),
+// w_iI * ap_i[delta(home(i), J)] over the children and their transfers to I in order.  Inactive
+// rows and non-canonical slots get zeros, as in the one-stage form.
+constexpr int GP = 128;
+template <class T> __global__ void __launch_bounds__(GP) k_mg_gal_pt(const __grid_constant__ Dev D, int l, int ex, int ey, int ez) {
+  grid_dep_wait(D.pdl_early);
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  __shared__ int ch_i[64];
+  __shared__ I3 ch_home[64];
+  __shared__ int ch_n[64];
+  __shared__ float ch_w[64][8];
+  const MG m(D);
+  const MGLevelDev& cl = D.lv[l + 1];
+  const int t = threadIdx.x, nch = ex * ey * ez;
+  for (int I = blockIdx.x; I < cl.count; I += gridDim.x) {  // uniform over the block
+    float* row = D.mgmat + cl.moff + (long long)I * 125;
+    if (!m.active<T>(l + 1, I)) {
+      if (t < 125) row[t] = 0.f;
+      continue;
+    }
+    const I3 qc = m.coord(l + 1, I);
+    if (t < nch) {
+      int lo[3], ext[3];
+      for (int a = 0; a < 3; a++) child_range(D, l, a, qc[a], lo[a], ext[a]);
+      const int gx = t % ex, gy = (t / ex) % ey, gz = t / (ex * ey);
+      I3 qi = mk(lo[0] + gx, lo[1] + gy, lo[2] + gz);
+      const MGLevelDev& fl = D.lv[l];
+      bool cell = m.wrap_q(l, qi);
+      const int i = cell ? qi.x + fl.nx * (qi.y + fl.ny * qi.z) : 0;
+      cell = cell && m.active<T>(l, i);
+      int n = 0;
+      if (cell) {
+        int li[8];
+        float lw[8];
+        const int nl = m.transfers(l, i, li, lw);
+        for (int a = 0; a < nl; a++)
+          if (li[a] == I) ch_w[t][n++] = lw[a];
+      }
+      ch_i[t] = i;
+      ch_n[t] = n;
+      ch_home[t] = mk(qi.x / fl.fx, qi.y / fl.fy, qi.z / fl.fz);
+    }
+    __syncthreads();
+    if (t < 125) {
+      const I3 d = mk(t % 5 - 2, (t / 5) % 5 - 2, t / 25 - 2);
+      I3 qj = addI(qc, d);
+      const bool in = m.wrap_q(l + 1, qj);
+      const int J = in ? qj.x + cl.nx * (qj.y + cl.ny * qj.z) : -1;
+      const bool canonical = in && J >= I && eqI(m.delta_q(l + 1, qc, qj), d);
+      float total = 0.f;
+      if (canonical)
+        for (int c = 0; c < nch; c++) {
+          const int n = ch_n[c];
+          if (n == 0) continue;
+          const I3 e = m.delta_q(l + 1, ch_home[c], qj);
+          if (abs(e.x) > 2 || abs(e.y) > 2 || abs(e.z) > 2) continue;
+          const float v = D.gal_ap[(long long)ch_i[c] * 125 + MG::slot(e)];
+          for (int a = 0; a < n; a++) total += ch_w[c][a] * v;
+        }
+      row[t] = canonical ? total : 0.f;
+    }
+    __syncthreads();
+  }
+}
+
 // ELL rows (pressure_multigrid.glslinc:176-182)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_constant__ Dev D, int l) {
   grid_dep_wait(D.pdl_early);
@@ -1046,6 +1183,23 @@ template <class T> __global__ void __launch_bounds__(1024) k_mg_bottom(const __g
 // `span` values, the ELL values and their columns as 16-bit indices, each part 16-byte aligned):
 // load, cycle, write the fields back.
 // Levels lb..L-1 staged in `stage` by one block, the sub-cycle run there, the fields written back.
+// dst[k] = src[at(k)] for k < n over the block, kStageU loads of a thread issued before its stores.
+constexpr int kStageU = 8;
+template <class D_, class S_, class F> DI void staged_copy(D_* dst, const S_* __restrict__ src, long long n, F at) {
+  for (long long k0 = threadIdx.x; k0 < n; k0 += (long long)kStageU * blockDim.x) {
+    S_ v[kStageU];
+#pragma unroll
+    for (int u = 0; u < kStageU; u++) {
+      const long long k = k0 + (long long)u * blockDim.x;
+      if (k < n) v[u] = src[at((int)k)];
+    }
+#pragma unroll
+    for (int u = 0; u < kStageU; u++) {
+      const long long k = k0 + (long long)u * blockDim.x;
+      if (k < n) dst[k] = (D_)v[u];
+    }
+  }
+}
 template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* stage, float* small) {
   const int L = D.L;
   const int span = D.lv[L - 1].off + D.lv[L - 1].count - D.lv[lb].off;
@@ -1056,17 +1210,16 @@ template <class T> DI void bottom_staged(const Dev& D, int lb, unsigned char* st
   // the dense coarse solve's factor (at most 64 x 64) after the columns
   const int nc = D.lv[L - 1].count;
   float* linv = (float*)((unsigned char*)cols + (((size_t)(e1 - e0) * 2 + 15) & ~(size_t)15));
-  if (nc <= 64)
-    for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) linv[k] = D.mglinv[k];
+  // every load of a thread's share is issued before its stores (kStageU in flight per array): a
+  // single block would otherwise wait out one memory latency per element it stages
+  if (nc <= 64) staged_copy(linv, D.mglinv, (long long)nc * nc, [](int k) { return k; });
   const T* gvec = (const T*)D.mgv + D.lv[lb].off;
-  for (int f = 0; f < 8; f++)
-    for (int k = threadIdx.x; k < span; k += blockDim.x) vec[f * span + k] = gvec[(size_t)f * D.mg_nodes + k];
+  const size_t nodes = (size_t)D.mg_nodes;
+  staged_copy(vec, gvec, 8LL * span, [span, nodes](int k) { return (size_t)(k / span) * nodes + (size_t)(k % span); });
   const T* gell = (const T*)D.mgell + e0;
   const int* gcol = D.mgcol + e0;
-  for (long long k = threadIdx.x; k < e1 - e0; k += blockDim.x) {
-    ell[k] = gell[k];
-    cols[k] = (unsigned short)gcol[k];
-  }
+  staged_copy(ell, gell, e1 - e0, [](int k) { return k; });
+  staged_copy(cols, gcol, e1 - e0, [](int k) { return k; });
   __syncthreads();
   bottom_cycle<T>(D, MGs(D, vec, ell, cols, nc <= 64 ? linv : D.mglinv, lb, span), lb, small);
   T* out = (T*)D.mgv + D.lv[lb].off;
@@ -1181,6 +1334,122 @@ __global__ void __launch_bounds__(CNT) k_mg_coarse(const __grid_constant__ Dev D
   }
 }
 
+// ---------------------------------------------------------------- coarse leg in one cluster
+// Levels lt..mg_bottom-1 of a V-cycle and the bottom sub-cycle in one launch of one thread-block
+// cluster (kLegCtas blocks of kLegThreads, on neighbouring SMs): the phases of Cycle::level for
+// those levels in the same order, with the same per-row functions as the per-level kernels
+// (product-parallel rows, products summed in stencil order, so the bits are those of
+// k_mgl_rows), separated by the cluster's hardware barrier instead of kernel boundaries.  The
+// rows of a level are split into kLegCtas contiguous ranges; block 0 runs the bottom sub-cycle
+// in its shared memory while the others wait at the barrier.  The barrier's release/acquire
+// semantics at cluster scope order every block's global-memory writes of one phase before the
+// reads of the next.  No wait is a spin: a cluster barrier completes once every thread of the
+// cluster has arrived, and every thread runs the same sequence of phases.
+constexpr int kLegCtas = 8;
+constexpr int kLegThreads = 1024;
+constexpr int kLegRowsMax = 1024;  // rows of one block's chunk (row indices and interior flags)
+
+DI void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <class T>
+__global__ void __launch_bounds__(kLegThreads, 1) k_mg_leg(const __grid_constant__ Dev D, int phase, int lt) {
+  grid_dep_wait(D.pdl_early);
+  if (!phase_on(D, phase)) return;  // the same decision in every block
+  extern __shared__ __align__(16) unsigned char dyn[];
+  __shared__ int lin[kMaxStencil];
+  __shared__ float small[64];
+  // dynamic shared memory: the products of a chunk, then its row indices and interior flags (the
+  // bottom stage of block 0 reuses all of it)
+  const int prod_cap = (D.mg_leg_smem - kLegRowsMax * (int)(sizeof(int) + sizeof(bool))) / (int)sizeof(float);
+  float* prod = (float*)dyn;
+  int* rowi = (int*)(dyn + (size_t)prod_cap * sizeof(float));
+  bool* inner = (bool*)(rowi + kLegRowsMax);
+  const MG m(D);
+  const int lb = D.mg_bottom;
+  const int nb = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+  int field[kMaxLevels];
+  // sweep op (0 Chebyshev, 1 Jacobi, 2 residual) over this block's range of the active rows
+  auto rows_op = [&](int l, int op, int a, int bb, int c) {
+    const MGLevelDev& lv = D.lv[l];
+    const int nrows = (int)D.mg_rowcount[l], S = lv.stencil, n = lv.count;
+    const bool need = !(op == 0 && c != 0) && !(op == 1 && bb != 0);
+    const int per = (nrows + nb - 1) / nb, r0 = b * per, r1 = min(nrows, r0 + per);
+    const int rc = max(1, min(kLegRowsMax, prod_cap / S));
+    for (int k = t; k < S; k += kLegThreads) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
+    const T* x = m.field<T>(a, l);
+    const T* ell = (const T*)D.mgell + lv.eoff;
+    const int* col = D.mgcol + lv.eoff;
+    for (int c0 = r0; c0 < r1; c0 += rc) {
+      const int cnt = min(rc, r1 - c0);
+      for (int r = t; r < cnt; r += kLegThreads) {
+        const int i = D.mg_rowlist[lv.off + c0 + r];
+        rowi[r] = i;
+        const I3 q = m.coord(l, i);
+        inner[r] = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
+      }
+      __syncthreads();
+      if (need) {
+#pragma unroll 4
+        for (int p = t; p < S * cnt; p += kLegThreads) {
+          const int k = p / cnt, r = p - k * cnt, i = rowi[r];
+          const long long e = (long long)k * n + i;
+          const int j = inner[r] ? i + lin[k] : __ldg(col + e);
+          prod[p] = ld_val(ell[e]) * ld_val(x[j]);
+        }
+        __syncthreads();
+      }
+      for (int r = t; r < cnt; r += kLegThreads) {
+        const int i = rowi[r];
+        float ax = 0.f;
+        if (need) {
+          if (!m.active<T>(l, i)) ax = ld_val(x[i]);
+          else {
+            float sum = 0.f;
+            for (int k = 0; k < S; k++) sum += prod[k * cnt + r];
+            ax = sum;
+          }
+        }
+        if (op == 0) cheb_update<T>(m, l, a, bb, i, c != 0, ax);
+        else if (op == 1) jacobi_update<T>(m, l, a, bb, i, ax);
+        else residual_update<T>(m, l, i, ax);
+      }
+      __syncthreads();
+    }
+    cluster_barrier();
+  };
+  auto smooth = [&](int l, int f, bool zero) {
+    for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
+      const bool first = zero && sweep == 0;
+      if (D.mg_smoother == 1) rows_op(l, 0, f, sweep + 1, first ? 1 : 0);
+      else rows_op(l, 1, f, first ? 1 : 0, 0);
+      f = 3 - f;
+    }
+    return f;
+  };
+  for (int l = lt; l < lb; l++) {
+    const int f = smooth(l, 1, true);
+    field[l] = f;
+    rows_op(l, 2, f, 0, 0);
+    for (int i = b * kLegThreads + t; i < D.lv[l + 1].count; i += nb * kLegThreads) restrict_cell<T>(m, l + 1, i);
+    cluster_barrier();
+  }
+  if (b == 0) {
+    if (D.mg_bottom_smem > 0) bottom_staged<T>(D, lb, dyn, small);
+    else bottom_cycle<T>(D, m, lb, small);
+  }
+  cluster_barrier();
+  int cf = 1;
+  for (int l = lb - 1; l >= lt; l--) {
+    const int f = field[l];
+    const int nrows = (int)D.mg_rowcount[l];
+    for (int r = b * kLegThreads + t; r < nrows; r += nb * kLegThreads) prolong_cell<T>(m, l, f, cf, D.mg_rowlist[D.lv[l].off + r]);
+    cluster_barrier();
+    cf = smooth(l, f, false);
+  }
+}
+
 // op 10 of the cycle + op 4 / op 9 finalisation (Jacobi smoothing path)
 template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __grid_constant__ Dev D, int phase, int f) {
   grid_dep_wait(D.pdl_early);
@@ -1256,6 +1525,33 @@ void coop_launch(void (*kernel)(KArgs...), unsigned blocks, unsigned threads, si
   cfg.numAttrs = 1;
   probed(kProbeAll, s, 0.0, [&] { cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...); });
 }
+// A launch of one thread-block cluster of `ctas` blocks (with programmatic serialization when
+// enabled), probed as `kind` with `bytes` tagged with `level`.
+template <class... KArgs, class... Args>
+void cluster_launch(void (*kernel)(KArgs...), unsigned ctas, unsigned threads, size_t smem, cudaStream_t s, int kind,
+                    double bytes, int level, Args&&... args) {
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 2 : 1;
+  probed(kind, s, bytes, [&] {
+    probed(kProbeAll, s, 0.0, [&] { cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...); });
+  }, level);
+}
+__global__ void k_cluster_probe(int* x) {
+  cluster_barrier();
+  if (threadIdx.x == 0 && blockIdx.x == 0) *x = 1;
+}
 __global__ void k_coop_probe(int* x) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *x = 1;
 }
@@ -1314,7 +1610,8 @@ template <class T> struct Cycle {
   // A level >= 1 reached through the regular per-level path has its first pre-smoothing sweep
   // done by the launch that restricts into it (k_mgl op 5).
   bool restrict_fused(int l) const {
-    return l >= 1 && l != D.L - 1 && l != D.mg_bottom && !(D.mg_coarse_from > 0 && l == D.mg_coarse_from && l < D.mg_bottom);
+    return l >= 1 && l != D.L - 1 && l != D.mg_bottom && !(D.mg_coarse_from > 0 && l == D.mg_coarse_from && l < D.mg_bottom) &&
+           !(D.mg_leg_from > 0 && l == D.mg_leg_from && l < D.mg_bottom);
   }
   // pre- and post-smoothing flip the field mg_smoothing times each: a level ends in field 1
   int bottom_field() const { return 1; }
@@ -1323,6 +1620,22 @@ template <class T> struct Cycle {
     if (D.mg_coarse_from > 0 && l == D.mg_coarse_from && l < D.mg_bottom) {
       const size_t smem = std::max((size_t)kMaxStencil * CRR * sizeof(float), (size_t)D.mg_bottom_smem);
       coop_launch((k_mg_coarse<T>), D.coarse_blocks, CNT, smem, s, D, phase, l);
+      int f = 1;  // the field logic of the kernel: pre- then post-smoothing from field 1
+      for (int k = 0; k < 2 * D.mg_smoothing; k++) f = 3 - f;
+      return f;
+    }
+    if (D.mg_leg_from > 0 && l == D.mg_leg_from && l < D.mg_bottom) {
+      // algorithmic bytes: the leg's level sweeps and residuals (the bottom's are not counted)
+      double bytes = 0.0;
+      for (int k = l; k < D.mg_bottom; k++) {
+        for (int sweep = 0; sweep < D.mg_smoothing; sweep++) {
+          const int op = D.mg_smoother == 1 ? 0 : 1;
+          bytes += level_op_bytes(D, k, op, op == 0 ? sweep + 1 : (sweep == 0 ? 1 : 0), op == 0 && sweep == 0 ? 1 : 0, sizeof(T));
+          bytes += level_op_bytes(D, k, op, op == 0 ? sweep + 1 : 0, 0, sizeof(T));
+        }
+        bytes += level_op_bytes(D, k, 2, 0, 0, sizeof(T));
+      }
+      cluster_launch((k_mg_leg<T>), kLegCtas, kLegThreads, (size_t)D.mg_leg_smem, s, kProbeLeg, bytes, l, D, phase, l);
       int f = 1;  // the field logic of the kernel: pre- then post-smoothing from field 1
       for (int k = 0; k < 2 * D.mg_smoothing; k++) f = 3 - f;
       return f;
@@ -1407,10 +1720,16 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
       ext[a] = (lv.aggregate || f == 1) ? f : ((periodic && nf <= 4) ? nf : 4);
     }
     (void)lo;
-    int G = ext[1] * ext[2], rpb = GT / G;
-    unsigned gr = (unsigned)((D.lv[l].count + rpb - 1) / rpb);
-    const int slots = D.lv[l].gal_slots > 0 ? D.lv[l].gal_slots : 125;
-    pdl_launch((k_mg_galerkin<T>), gr, GT, (size_t)slots * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
+    if (l - 1 >= 1) {
+      // from a fine level >= 1: A P per active fine row, then P^T (A P) per coarse row
+      pdl_launch((k_mg_gal_ap<T>), (unsigned)((D.lv[l - 1].count + GA - 1) / GA), GA, (size_t)125 * GA * sizeof(float), s, D, l - 1);
+      pdl_launch((k_mg_gal_pt<T>), (unsigned)D.lv[l].count, GP, 0, s, D, l - 1, ext[0], ext[1], ext[2]);
+    } else {
+      int G = ext[1] * ext[2], rpb = GT / G;
+      unsigned gr = (unsigned)((D.lv[l].count + rpb - 1) / rpb);
+      const int slots = D.lv[l].gal_slots > 0 ? D.lv[l].gal_slots : 125;
+      pdl_launch((k_mg_galerkin<T>), gr, GT, (size_t)slots * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
+    }
     pdl_launch((k_mg_scale<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   }
   for (int l = 1; l < D.L; l++) pdl_launch((k_mg_ell<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
@@ -1464,6 +1783,83 @@ int coarse_blocks(size_t smem) {
   if (x) cudaFree(x);
   cudaGetLastError();
   return ok ? sms : 0;
+}
+
+bool leg_available(size_t smem) {
+  if (smem > (size_t)kBottomSmemMax) return false;
+  if (cudaFuncSetAttribute(k_mg_leg<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax) != cudaSuccess ||
+      cudaFuncSetAttribute(k_mg_leg<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBottomSmemMax) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchAttribute cl[1];
+  cl[0].id = cudaLaunchAttributeClusterDimension;
+  cl[0].val.clusterDim.x = kLegCtas;
+  cl[0].val.clusterDim.y = 1;
+  cl[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t occ = {};
+  occ.gridDim = dim3(kLegCtas);
+  occ.blockDim = dim3(kLegThreads);
+  occ.dynamicSmemBytes = smem;
+  occ.attrs = cl;
+  occ.numAttrs = 1;
+  int n32 = 0, n16 = 0;
+  if (cudaOccupancyMaxActiveClusters(&n32, k_mg_leg<float>, &occ) != cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&n16, k_mg_leg<__nv_bfloat16>, &occ) != cudaSuccess || n32 < 1 || n16 < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  // the launch form the cycle uses (cluster dimension, programmatic serialization), run once on a
+  // stream and once from the body of a conditional graph node, as the CG loop's graphs hold it
+  int* x = nullptr;
+  cudaStream_t s = nullptr;
+  cudaGraph_t g = nullptr, body_out = nullptr;
+  cudaGraphExec_t e = nullptr;
+  bool ok = cudaMalloc(&x, sizeof(int)) == cudaSuccess && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
+  cudaLaunchAttribute attr[2];
+  attr[0] = cl[0];
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kLegCtas);
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 2 : 1;
+  int got = 0;
+  ok = ok && cudaMemsetAsync(x, 0, sizeof(int), s) == cudaSuccess && cudaLaunchKernelEx(&cfg, k_cluster_probe, x) == cudaSuccess &&
+       cudaMemcpyAsync(&got, x, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess &&
+       got == 1;
+  ok = ok && cudaMemsetAsync(x, 0, sizeof(int), s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess &&
+       cudaGraphCreate(&g, 0) == cudaSuccess;
+  if (ok) {
+    cudaGraphConditionalHandle hc;
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    cudaGraphNode_t node;
+    ok = cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    if (ok) {
+      p.conditional.handle = hc;
+      p.conditional.type = cudaGraphCondTypeIf;
+      p.conditional.size = 1;
+      ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p) == cudaSuccess;
+    }
+    if (ok && cudaStreamBeginCaptureToGraph(s, p.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                  cudaSuccess) {
+      const bool launched = cudaLaunchKernelEx(&cfg, k_cluster_probe, x) == cudaSuccess;
+      ok = cudaStreamEndCapture(s, &body_out) == cudaSuccess && launched;
+    } else
+      ok = false;
+    got = 0;
+    ok = ok && cudaGraphInstantiate(&e, g, 0) == cudaSuccess && cudaGraphLaunch(e, s) == cudaSuccess &&
+         cudaMemcpyAsync(&got, x, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess &&
+         got == 1;
+  }
+  if (e) cudaGraphExecDestroy(e);
+  if (g) cudaGraphDestroy(g);
+  if (s) cudaStreamDestroy(s);
+  if (x) cudaFree(x);
+  cudaGetLastError();
+  return ok;
 }
 
 void mg_kernel_attributes() {

@@ -23,7 +23,8 @@ enum ProbeKind {
   kProbeAll = 5,        // every kernel of the trial (bytes not counted)
   kProbeEmpty = 6,      // calibration: an empty kernel bracketed as a probed launch is (kind + all)
   kProbeEmptyInner = 7, // the inner bracket of that calibration
-  kProbeCount = 8
+  kProbeLeg = 8,        // k_mg_leg, the coarse levels and the bottom of a V-cycle in one cluster
+  kProbeCount = 9
 };
 // `level` >= 1 marks a multigrid level sweep whose bytes were counted over all rows of the level;
 // the probe scales them to the rows the sweep visits (the active rows) once the trial has run.
@@ -122,6 +123,11 @@ void launch_mg_build(const Dev& D, cudaStream_t s);
 void launch_mg_vcycle(const Dev& D, cudaStream_t s, int phase);
 void mg_kernel_attributes();
 int coarse_blocks(size_t smem);  // blocks of the one-launch coarse V-cycle, 0 when unavailable
+// Whether the one-cluster coarse leg can run with `smem` bytes of dynamic shared memory per block
+// (a cluster of that shape fits the device, and such a launch can be captured into a graph).
+bool leg_available(size_t smem);
+constexpr int kLegRowsFrom = 8192;  // the leg starts at the first level with at most this many rows
+constexpr size_t kLegSmemMin = 100 * 1024;
 void launch_mg_cols(const Dev& D, cudaStream_t s);
 // k_init.cu
 void launch_initial(const Dev& D, cudaStream_t s, float4* probes);

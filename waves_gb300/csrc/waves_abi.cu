@@ -344,12 +344,17 @@ waves_status setup_device(waves_handle* h) {
     // domain edge (where donors take the boundary path), every column when x is periodic.
     const int cx = D.nx + 1, cy = D.ny + 1;
     std::vector<unsigned char> cls((size_t)3 * cx * cy, 1);
+    // faces within `band` cells of a solid cell or the domain edge go straight to the general
+    // pass; the others try the fast pass, which hands over every face whose samples leave the
+    // fast path (so the band only moves work between the passes; the results do not depend on it)
+    int band = 3;
+    if (const char* e = getenv("WAVES_MAC_BAND")) band = std::max(0, std::min(3, atoi(e)));
     if (!D.px)
       for (int y = 0; y < cy; y++)
         for (int x = 0; x < cx; x++) {
-          bool edge = x < 3 || x > D.nx - 4 || y < 3 || y > D.ny - 4;
-          for (int dy = -3; dy <= 3 && !edge; dy++)
-            for (int dx = -3; dx <= 3 && !edge; dx++) edge = solid_host(k, x + dx, y + dy);
+          bool edge = x < band || x > D.nx - 1 - band || y < band || y > D.ny - 1 - band;
+          for (int dy = -band; dy <= band && !edge; dy++)
+            for (int dx = -band; dx <= band && !edge; dx++) edge = solid_host(k, x + dx, y + dy);
           for (int a = 0; a < 3; a++) cls[((size_t)a * cy + y) * cx + x] = edge ? 1 : 0;
         }
     unsigned char* dcls;
@@ -627,7 +632,40 @@ waves_status setup_device(waves_handle* h) {
     }
     AL(D.gbar, 2, false, "grid_barrier");
   }
+  {
+    // WAVES_MG_LEG=1: the coarse leg (the levels with at most kLegRowsFrom rows above the
+    // bottom, and the bottom) runs as one launch of one thread-block cluster instead of a launch
+    // per sweep, restriction and prolongation.  Off by default: on the beach (leg = level 3,
+    // 4,680 rows, and the bottom) it is slower than the per-level launches (17.32 vs 16.98 ms per
+    // step at t = 5 s): each of its ten phases waits out several dependent global-memory round
+    // trips on eight SMs, about 98 us per V-cycle in all.
+    D.mg_leg_from = 0;
+    D.mg_leg_smem = 0;
+    bool want = false;
+    if (const char* e = getenv("WAVES_MG_LEG")) want = D.mg_coarse_from == 0 && atoi(e) != 0;
+    int from = 0;
+    for (int l = 1; want && l < D.mg_bottom; l++)
+      if (D.lv[l].count <= wg::kLegRowsFrom) {
+        from = l;
+        break;
+      }
+    if (from > 0) {
+      wg::mg_kernel_attributes();
+      const size_t smem = std::max(wg::kLegSmemMin, (size_t)D.mg_bottom_smem);
+      if (wg::leg_available(smem)) {
+        D.mg_leg_from = from;
+        D.mg_leg_smem = (int)smem;
+      }
+    }
+  }
   AL(D.mgmat, moff, true, "mg_matrix");
+  {
+    // A P of the two-stage Galerkin product, 125 slots per row of the largest fine level >= 1
+    // that is coarsened (dense by fine cell; only active rows are written and read)
+    long long ap_rows = 1;
+    for (int l = 1; l + 1 < D.L; l++) ap_rows = std::max(ap_rows, (long long)D.lv[l].count);
+    AL(D.gal_ap, (size_t)ap_rows * 125, false, "galerkin_ap");
+  }
   {
     void* p;
     if ((st = alloc(h, &p, (size_t)eoff * tsz, true, "mg_ell")) != WAVES_OK) return st;
