@@ -461,6 +461,23 @@ DI void block_reduce_k(const double (&vals)[K], const int (&ops)[K], double* sh,
   __syncthreads();
 }
 
+// The last block's pass over nb per-block partials of one component: thread t combines partials
+// t, t + NT, t + 2 NT, ... in that order (sum, op 0, or maximum), with kPartU loads issued before
+// their additions, so the thread waits out one memory latency per kPartU partials, not per partial.
+constexpr int kPartU = 4;
+template <int NT> DI double partials_in_order(const double* part, int nb, int op) {
+  double acc = op == 0 ? 0.0 : -1e300;
+  for (int b0 = threadIdx.x; b0 < nb; b0 += kPartU * NT) {
+    double p[kPartU];
+#pragma unroll
+    for (int u = 0; u < kPartU; u++) p[u] = b0 + u * NT < nb ? __ldcg(&part[b0 + u * NT]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < kPartU; u++)
+      if (b0 + u * NT < nb) acc = op == 0 ? acc + p[u] : (acc < p[u] ? p[u] : acc);
+  }
+  return acc;
+}
+
 // Write `K` per-block partials (double), then let the last block to finish reduce all partials
 // in a fixed order.  Returns true in every thread of the last block, with the totals in `out`.
 // `ops[k]` selects 0 = sum, 1 = max for each component.
@@ -485,13 +502,7 @@ DI bool last_block_reduce(const Dev& D, int site, double (&vals)[K], const int (
   __threadfence();
   double acc[K];
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    acc[k] = ops[k] == 0 ? 0.0 : -1e300;
-    for (int b = threadIdx.x; b < nb; b += NT) {
-      double p = __ldcg(&part[(size_t)k * nb + b]);
-      acc[k] = ops[k] == 0 ? acc[k] + p : (acc[k] < p ? p : acc[k]);
-    }
-  }
+  for (int k = 0; k < K; k++) acc[k] = partials_in_order<NT>(part + (size_t)k * nb, nb, ops[k]);
   block_reduce_k<NT, K>(acc, ops, sh, tot);
 #pragma unroll
   for (int k = 0; k < K; k++) out[k] = tot[k];
@@ -565,13 +576,7 @@ DI bool last_block_reduce_mf(const Dev& D, int site, const double* vals, const i
   if constexpr (KD > 0) {
     double acc[KD];
 #pragma unroll
-    for (int k = 0; k < KD; k++) {
-      acc[k] = opk[k] == 0 ? 0.0 : -1e300;
-      for (int b = threadIdx.x; b < nb; b += NT) {
-        double p = __ldcg(&part[(size_t)k * nb + b]);
-        acc[k] = opk[k] == 0 ? acc[k] + p : (acc[k] < p ? p : acc[k]);
-      }
-    }
+    for (int k = 0; k < KD; k++) acc[k] = partials_in_order<NT>(part + (size_t)k * nb, nb, opk[k]);
     block_reduce_k<NT, KD>(acc, opk, sh, tot);
 #pragma unroll
     for (int k = 0; k < KD; k++) out[k] = tot[k];
@@ -580,9 +585,13 @@ DI bool last_block_reduce_mf(const Dev& D, int site, const double* vals, const i
 #pragma unroll
   for (int k = 0; k < KF; k++) {
     accf[k] = -INFINITY;
-    for (int b = threadIdx.x; b < nb; b += NT) {
-      const float p = __ldcg(&partf[(size_t)k * nb + b]);
-      accf[k] = accf[k] < p ? p : accf[k];
+    // kPartU loads in flight per thread; maxima do not depend on the order anyway
+    for (int b0 = threadIdx.x; b0 < nb; b0 += kPartU * NT) {
+      float p[kPartU];
+#pragma unroll
+      for (int u = 0; u < kPartU; u++) p[u] = b0 + u * NT < nb ? __ldcg(&partf[(size_t)k * nb + b0 + u * NT]) : -INFINITY;
+#pragma unroll
+      for (int u = 0; u < kPartU; u++) accf[k] = accf[k] < p[u] ? p[u] : accf[k];
     }
   }
   block_max_f<NT, KF>(accf, shw, totf);

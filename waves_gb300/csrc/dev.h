@@ -118,6 +118,9 @@ struct Dev {
                                  // the general pass, op 27 / op 28 cursors of the fast pass, op 27 / op 28
                                  // counts of faces the fast pass handed over
   int* mac_ovf;                  // faces the fast pass handed over to the general pass
+  int* geo_queue;                // cells of op 18 that need the neighbourhood search
+  unsigned* geo_qcount;          // their count (reset by op 17)
+  int geo_seed_grid;             // blocks of the search pass (persistent, grid-stride)
   int mac_grid;                  // persistent MacCormack blocks (3 per SM form)
   int mac_grid2;                 // the same, 2 per SM form
   int mac_fast_grid;             // persistent blocks of the interior fast-path pass

@@ -144,7 +144,54 @@ struct Geo {
     }
     return best;
   }
-  // geometry_distance (pressure_geometry.glslinc:120-145)
+  // geometry_distance (pressure_geometry.glslinc:120-145) up to the neighbourhood search: the
+  // distance, or *search = true where the cell needs the 27-neighbour search (seed_terms and the
+  // ordered replay in k_geom_seed finish it)
+  DI float distance_or_search(I3 q, bool* search) const {
+    float f = gfrac(q);
+    F3 hh = hvec();
+    *search = false;
+    if (f > 0.f && f < 1.f) {
+      float4 eq = D.plane[g.index3(q)];
+      F3 e3 = mf(eq.x, eq.y, eq.z);
+      return (half_dot(e3) - eq.w) / len3(div3(e3, hh));
+    }
+    bool needs_seed = false;
+    for (int axis = 0; axis < 3; axis++)
+      for (int sign = -1; sign <= 1; sign += 2) {
+        I3 nb = g.wrap_cell(ax(q, axis, sign));
+        if (g.solid(nb) || g.outside(nb)) continue;
+        float other = gfrac(nb);
+        bool inside = other >= 1.f;
+        if (other > 0.f && other < 1.f) {
+          float4 eq = D.plane[g.index3(nb)];
+          inside = half_dot(mf(eq.x, eq.y, eq.z)) < eq.w;
+        }
+        if (inside != (f >= 1.f)) needs_seed = true;
+      }
+    if (!needs_seed) return (f >= 1.f ? -1.f : 1.f) * len3(hh) * 4.f;
+    *search = true;
+    return 0.f;
+  }
+  // One neighbour (x, y, z) of the search of geometry_distance: false where it is skipped (outside
+  // the domain or solid); else its lower bound lb (the distance to its box) and the values the
+  // search takes the minimum of, in its order: the polygon distance (where the neighbour holds an
+  // interface, has_poly) and the three transition distances.
+  DI bool seed_terms(I3 q, int x, int y, int z, float& lb, bool& has_poly, float v[4]) const {
+    const F3 hh = hvec();
+    const I3 neighbor = addI(q, mk(x, y, z)), wrapped = g.wrap_cell(neighbor);
+    if (g.outside(wrapped) || g.solid(wrapped)) return false;
+    const float fraction = gfrac(wrapped);
+    const I3 dq = subI(q, neighbor);
+    const F3 point = mf(((float)dq.x + .5f) * hh.x, ((float)dq.y + .5f) * hh.y, ((float)dq.z + .5f) * hh.z);
+    const F3 cl = mf(clampf_(point.x, 0.f, hh.x), clampf_(point.y, 0.f, hh.y), clampf_(point.z, 0.f, hh.z));
+    lb = len3(sub3(point, cl));
+    has_poly = fraction > 0.f && fraction < 1.f;
+    v[0] = has_poly ? polygon_distance(point, D.plane[g.index3(wrapped)]) : 0.f;
+    for (int axis = 0; axis < 3; axis++) v[1 + axis] = transition_distance(point, neighbor, axis);
+    return true;
+  }
+  // geometry_distance (pressure_geometry.glslinc:120-145), the sequential form
   DI float distance(I3 q) const {
     float f = gfrac(q);
     F3 hh = hvec();
@@ -231,6 +278,7 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
   Geo G(D, op);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
   float v[2] = {-INFINITY, -INFINITY};
+  if (op == 17 && on && i == 0) D.geo_qcount[0] = 0u;  // the search queue of k_geom_phi
   if (i < D.N) {
     if (on) D.plane[i] = G.reconstruct(G.g.coord(i));
     if (bounds) {
@@ -252,16 +300,72 @@ __global__ void __launch_bounds__(NT) k_geom_plane(const __grid_constant__ Dev D
 }
 
 // ---------------------------------------------------------------- op 18
+// Every cell but those that need the neighbourhood search, which are queued for k_geom_seed (the
+// queue's count is reset by k_geom_plane, op 17, which runs first).  A warp of this pass would
+// otherwise wait for its few searching lanes.
 __global__ void __launch_bounds__(NT, 6) k_geom_phi(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!geometry_on(D)) return;
   Geo G(D, 18);
   long long i = (long long)blockIdx.x * NT + threadIdx.x;
-  if (i >= D.N) return;
-  I3 q = G.g.coord(i);
-  float ph = G.distance(q);
-  D.phi[i] = ph;
-  D.kind[i] = G.g.solid(q) ? -1 : (ph < 0.f ? 1 : 0);
+  bool search = false;
+  if (i < D.N) {
+    I3 q = G.g.coord(i);
+    float ph = G.distance_or_search(q, &search);
+    if (!search) {
+      D.phi[i] = ph;
+      D.kind[i] = G.g.solid(q) ? -1 : (ph < 0.f ? 1 : 0);
+    }
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, search);
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0 && ballot) base = atomicAdd(D.geo_qcount, (unsigned)__popc(ballot));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (search) D.geo_queue[base + __popc(ballot & ((1u << lane) - 1u))] = (int)i;
+}
+// The neighbourhood search of the queued cells, one warp per cell: lane n < 27 evaluates
+// neighbour n (x, y, z from -1 to 1, z fastest: the search's own order); lane 0 then replays the
+// search in that order with the same pruning test and the same minimum operations, so the
+// distance is the sequential search's bit for bit.
+constexpr int kSeedWarps = NT / 32;
+__global__ void __launch_bounds__(NT) k_geom_seed(const __grid_constant__ Dev D) {
+  grid_dep_wait(D.pdl_early);
+  if (!geometry_on(D)) return;
+  __shared__ float sv[kSeedWarps][27][5];
+  __shared__ unsigned char sflag[kSeedWarps][27];  // bit 0: evaluated, bit 1: has a polygon
+  Geo G(D, 18);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned total = *D.geo_qcount;
+  for (unsigned k = blockIdx.x * kSeedWarps + w; k < total; k += gridDim.x * kSeedWarps) {  // uniform over the warp
+    const int i = D.geo_queue[k];
+    const I3 q = G.g.coord(i);
+    if (lane < 27) {
+      float lb = 0.f, v[4] = {0.f, 0.f, 0.f, 0.f};
+      bool hp = false;
+      const bool ok = G.seed_terms(q, lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1, lb, hp, v);
+      sv[w][lane][0] = lb;
+      for (int j = 0; j < 4; j++) sv[w][lane][1 + j] = v[j];
+      sflag[w][lane] = (ok ? 1 : 0) | (hp ? 2 : 0);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const float f = G.gfrac(q);
+      const F3 hh = G.hvec();
+      float best = len3(hh) * 4.f;
+      for (int n = 0; n < 27; n++) {
+        const unsigned fl = sflag[w][n];
+        if (!(fl & 1u)) continue;
+        if (sv[w][n][0] >= best) continue;
+        if (fl & 2u) best = mnf(best, sv[w][n][1]);
+        for (int axis = 0; axis < 3; axis++) best = mnf(best, sv[w][n][2 + axis]);
+      }
+      const float ph = (f >= 1.f ? -1.f : 1.f) * best;
+      D.phi[i] = ph;
+      D.kind[i] = G.g.solid(q) ? -1 : (ph < 0.f ? 1 : 0);
+    }
+    __syncwarp();
+  }
 }
 
 // ---------------------------------------------------------------- op 16
@@ -767,6 +871,7 @@ void launch_coastal(const Dev& D, cudaStream_t s) {
 void launch_geometry(const Dev& D, cudaStream_t s) {
   pdl_launch(k_geom_plane, grid_for(D.N), NT, 0, s, D, 17, D.coastal);
   pdl_launch(k_geom_phi, grid_for(D.N), NT, 0, s, D);
+  pdl_launch(k_geom_seed, D.geo_seed_grid, NT, 0, s, D);
   pdl_launch(k_geom_coef, grid_for(D.N), NT, 0, s, D);
 }
 void launch_proj_setup(const Dev& D, cudaStream_t s) { pdl_launch(k_proj_setup, grid_for(D.S), NT, 0, s, D); }

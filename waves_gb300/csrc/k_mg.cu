@@ -555,19 +555,34 @@ template <class T> __global__ void __launch_bounds__(GT) k_mg_galerkin(const __g
       }
     }
   }
+  // the rows' activity and coordinates once per row (not once per slot): an inactive row, most of
+  // a coarse level, only stores its zeros
+  __shared__ bool ract[GT];
+  __shared__ I3 rq[GT];
+  if (t < rpb) {
+    const int row = blockIdx.x * rpb + t;
+    ract[t] = row < cl.count && m.active<T>(l + 1, row);
+    rq[t] = row < cl.count ? m.coord(l + 1, row) : mk(0, 0, 0);
+  }
   __syncthreads();
   for (int u = t; u < rpb * 125; u += GT) {
     int rl = u / 125, s = u % 125;
     int row = blockIdx.x * rpb + rl;
     if (row >= cl.count) continue;
-    float total = 0.f;
-    const int cs = cslot[s];
-    if (cs >= 0)
-      for (int gg = 0; gg < G; gg++) total += part[cs * GT + rl * G + gg];
-    I3 d = mk(s % 5 - 2, (s / 5) % 5 - 2, s / 25 - 2);
-    int J = m.wrap(l + 1, addI(m.coord(l + 1, row), d));
-    bool canonical = J >= row && eqI(m.delta(l + 1, row, J), d) && m.active<T>(l + 1, row);
-    D.mgmat[cl.moff + (long long)row * 125 + s] = canonical ? total : 0.f;
+    float out = 0.f;
+    if (ract[rl]) {
+      float total = 0.f;
+      const int cs = cslot[s];
+      if (cs >= 0)
+        for (int gg = 0; gg < G; gg++) total += part[cs * GT + rl * G + gg];
+      const I3 d = mk(s % 5 - 2, (s / 5) % 5 - 2, s / 25 - 2);
+      I3 qj = addI(rq[rl], d);
+      const bool in = m.wrap_q(l + 1, qj);
+      const int J = in ? qj.x + cl.nx * (qj.y + cl.ny * qj.z) : -1;
+      const bool canonical = J >= row && eqI(m.delta_q(l + 1, rq[rl], qj), d);
+      out = canonical ? total : 0.f;
+    }
+    D.mgmat[cl.moff + (long long)row * 125 + s] = out;
   }
 }
 // Galerkin product from a fine level l >= 1 in two stages (the oracle's mg_galerkin_ap and
@@ -901,12 +916,14 @@ template <class T, class M> DI void coarse_block(const M& m, int l, float* small
   const float* linv = m.coarse_inverse();
   if (t < n) {
     float d = 0.f;
+#pragma unroll 8
     for (int j = 0; j <= t; j++) d += linv[t * n + j] * ld_val(b[j]);
     small[t] = d;
   }
   __syncthreads();
   if (t < n) {
     float d = 0.f;
+#pragma unroll 8
     for (int j = t; j < n; j++) d += linv[j * n + t] * small[j];
     m.template field<T>(1, l)[t] = st_val<T>(d);
   }
@@ -1125,6 +1142,8 @@ struct MGs : MG {
     const T* e = (const T*)ell + at;
     const unsigned short* c = cols + at;
     float sum = 0.f;
+    // unrolled so that the shared-memory loads run ahead of the additions (which stay in order)
+#pragma unroll 9
     for (int k = 0; k < lv.stencil; k++) sum += ld_val(e[k * lv.count + i]) * ld_val(x[c[k * lv.count + i]]);
     return sum;
   }
