@@ -3,11 +3,13 @@
 // pressure_hierarchy_state.glsl; command order water/pressure_multigrid.gd:121-176).
 //
 // Storage type T is float (FP32 multigrid) or __nv_bfloat16 (BF16 storage and smoothing); every
-// arithmetic operation is FP32.  The Galerkin product is a deterministic gather: for coarse row I,
-// each thread of a group (the children of I in one (y, z) fine row) accumulates
-// (a_ij * w_iI) * w_jJ into its own shared-memory row of 125 slots, and the row is the sum of the
-// group partials in group order.  No float atomics touch any result.
+// arithmetic operation is FP32.  The Galerkin product is a deterministic gather.  From level 0:
+// for coarse row I, each thread of a group (the children of I in one (y, z) fine row) accumulates
+// (a_ij * w_iI) * w_jJ into its own shared-memory row of slots, and the row is the sum of the group
+// partials in group order.  From a level >= 1: A P per active fine row, then P^T (A P) per coarse
+// row (k_mg_gal_ap, k_mg_gal_pt).  No float atomics touch any result.
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -175,6 +177,38 @@ struct MG {
         size++;
       }
     return size;
+  }
+  // apply() of a level >= 1 whose stencil has at most SMAX entries, with every load of the row
+  // (its activity, the S operator values, the S neighbour values, and for a row near the level's
+  // edge the S cached columns first) issued before the first addition; the sum is then formed in
+  // stencil order, as apply() forms it, so the value is the same.  A sweep of a large level has
+  // few active rows per SM, and this turns the row's three or four dependent memory round trips
+  // into one or two.
+  template <class T, int SMAX> DI float apply_wide(int l, int f, int i, const int* lin_s) const {
+    const T* x = field<T>(f, l);
+    const MGLevelDev& lv = D.lv[l];
+    const int S = lv.stencil;
+    const T* ell = (const T*)D.mgell + lv.eoff;
+    const I3 q = coord(l, i);
+    const bool inner = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
+    const bool act = active<T>(l, i);
+    const float here = ld_val(x[i]);
+    const int* col = D.mgcol + lv.eoff;
+    float e[SMAX], v[SMAX];
+#pragma unroll
+    for (int k = 0; k < SMAX; k++)
+      if (k < S) {
+        const long long at = (long long)k * lv.count + i;
+        const int j = inner ? i + lin_s[k] : __ldg(col + at);
+        e[k] = ld_val(ell[at]);
+        v[k] = ld_val(x[j]);
+      }
+    if (!act) return here;
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < SMAX; k++)
+      if (k < S) sum += e[k] * v[k];
+    return sum;
   }
   // apply (pressure_multigrid.glslinc:90-105) with the V-cycle operators; `lin_s` (optional) is a
   // copy of the level's linear stencil offsets in shared memory.
@@ -862,12 +896,21 @@ template <class T, class M> DI void restrict_cell(const M& m, int l, int i) {
   I3 qc = m.coord(l, i);
   if (m.template active<T>(l, i)) {
     if (pv.aggregate) {
-      for (int z = 0; z < pv.fz; z++)
-        for (int y = 0; y < pv.fy; y++)
-          for (int x = 0; x < pv.fx; x++) {
-            int j = m.wrap(parent, mk(qc.x * pv.fx + x, qc.y * pv.fy + y, qc.z * pv.fz + z));
-            if (m.template active<T>(parent, j)) sum += ld_val(r6[j]);
-          }
+      // the (at most 2 x 2 x 2) children's flags and residuals loaded before the additions, which
+      // follow in the (z, y, x) order
+      bool act[8];
+      float rv[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const int x = c & 1, y = (c >> 1) & 1, z = c >> 2;
+        const bool in = x < pv.fx && y < pv.fy && z < pv.fz;
+        const int j = in ? m.wrap(parent, mk(qc.x * pv.fx + x, qc.y * pv.fy + y, qc.z * pv.fz + z)) : -1;
+        act[c] = in && m.template active<T>(parent, j);
+        rv[c] = j >= 0 ? ld_val(r6[j]) : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (act[c]) sum += rv[c];
     } else {
       const int* ix = D.rt_idx + cv.roff[0] + 4 * qc.x;
       const int* iy = D.rt_idx + cv.roff[1] + 4 * qc.y;
@@ -875,19 +918,29 @@ template <class T, class M> DI void restrict_cell(const M& m, int l, int i) {
       const float* wx = D.rt_w + cv.roff[0] + 4 * qc.x;
       const float* wy = D.rt_w + cv.roff[1] + 4 * qc.y;
       const float* wz = D.rt_w + cv.roff[2] + 4 * qc.z;
-      for (int tz = 0; tz < cv.rext[2]; tz++)
-        for (int ty = 0; ty < cv.rext[1]; ty++) {
-          int fy = iy[ty];
-          if (fy < 0) continue;
-          for (int tx = 0; tx < cv.rext[0]; tx++) {
-            int fx = ix[tx];
-            if (fx < 0) continue;
-            int j = fx + pv.nx * (fy + pv.ny * iz[tz]);
-            if (!m.template active<T>(parent, j)) continue;
-            float weight = 1.f * wx[tx] * wy[ty] * wz[tz];
-            sum += weight * ld_val(r6[j]);
+      // per plane of the children box (at most 4 x 4), every activity flag and residual is loaded
+      // before the additions, which follow in the (ty, tx) order with the same weights
+      for (int tz = 0; tz < cv.rext[2]; tz++) {
+        bool act[4][4];
+        float rv[4][4];
+#pragma unroll
+        for (int ty = 0; ty < 4; ty++)
+#pragma unroll
+          for (int tx = 0; tx < 4; tx++) {
+            const bool ok = ty < cv.rext[1] && tx < cv.rext[0] && iy[ty] >= 0 && ix[tx] >= 0;
+            const int j = ok ? ix[tx] + pv.nx * (iy[ty] + pv.ny * iz[tz]) : 0;
+            act[ty][tx] = ok && m.template active<T>(parent, j);
+            rv[ty][tx] = ld_val(r6[j]);
           }
-        }
+#pragma unroll
+        for (int ty = 0; ty < 4; ty++)
+#pragma unroll
+          for (int tx = 0; tx < 4; tx++)
+            if (act[ty][tx]) {
+              float weight = 1.f * wx[tx] * wy[ty] * wz[tz];
+              sum += weight * rv[ty][tx];
+            }
+      }
     }
   }
   m.template field<T>(0, l)[i] = st_val<T>(sum);
@@ -1053,6 +1106,7 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
 }
 
 // Generic levels (l >= 1): one thread per cell.
+constexpr int kWideStencil = 40;
 template <class T, int NTB = NT>
 __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   grid_dep_wait(D.pdl_early);
@@ -1071,10 +1125,17 @@ __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int 
   } else if (i >= D.lv[l].count)
     return;
   MG m(D);
+  // the one-thread-per-row FP32 sweeps (128-thread blocks) of a level with a stencil of at most
+  // kWideStencil entries issue the row's loads together (apply_wide; the BF16 form would spill)
+  auto ax = [&]() {
+    if constexpr (NTB == 128 && std::is_same<T, float>::value)
+      if (l >= 1 && D.lv[l].stencil <= kWideStencil) return m.apply_wide<T, kWideStencil>(l, a, i, lin_s);
+    return m.apply<T>(l, a, i, lin_s);
+  };
   switch (op) {
-    case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : m.apply<T>(l, a, i, lin_s)); break;
-    case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : m.apply<T>(l, a, i, lin_s)); break;
-    case 2: residual_update<T>(m, l, i, m.apply<T>(l, a, i, lin_s)); break;
+    case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : ax()); break;
+    case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : ax()); break;
+    case 2: residual_update<T>(m, l, i, ax()); break;
     case 3: restrict_cell<T>(m, l, i); break;
     case 4: prolong_cell<T>(m, l, a, b, i); break;
     case 5:
