@@ -10,6 +10,8 @@ constexpr int kMaxLevels = 12;
 constexpr int kMaxStencil = 125;
 constexpr int kBottomSmemMax = 200 * 1024;  // shared-memory stage of the bottom levels
 constexpr int kSolidPad = 16;  // margin of the tabulated solid() lookup
+constexpr int kDonorWall = -1;  // donor table: a solid cell on one side of the face only
+constexpr int kDonorNone = -2;  // donor table: solid on both sides, no mirror face
 
 // Indices into the double control block beyond the reference's 96 entries.
 enum CtrlExtra {
@@ -118,6 +120,8 @@ struct Dev {
                                  // the general pass, op 27 / op 28 cursors of the fast pass, op 27 / op 28
                                  // counts of faces the fast pass handed over
   int* mac_ovf;                  // faces the fast pass handed over to the general pass
+  int* mac_dtab;                 // per face, the donor of its solid neighbourhood (static geometry):
+                                 // kDonorWall, kDonorNone, or 2 f (+1 with parity -1) of the face read
   int* geo_queue;                // cells of op 18 that need the neighbourhood search
   unsigned* geo_qcount;          // their count (reset by op 17)
   int geo_seed_grid;             // blocks of the search pass (persistent, grid-stride)

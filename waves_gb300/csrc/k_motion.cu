@@ -349,22 +349,33 @@ struct Mac {
       valid = false;
       return 0.f;
     }
-    bool left = g.solid(ax(q, axis, -1)), right = g.solid(q);
-    if (left != right) {
+    // the face's solid neighbourhood, tabulated once from the static geometry (k_mac_donor_table:
+    // the same tests and the same reflect_voxel_donor search)
+    const int code = D.mac_dtab[g.face_local(q, axis)];
+    if (code == kDonorWall) {  // a solid cell on one side only
       valid = true;
       return 0.f;
     }
-    if (left && right) {
-      float reflection;
-      if (!reflect(q, axis, reflection)) {
-        valid = false;
-        return 0.f;
-      }
-      parity *= reflection;
+    if (code == kDonorNone) {  // solid on both sides and no mirror face
+      valid = false;
+      return 0.f;
     }
-    long long f = g.face_local(q, axis);
+    if (code & 1) parity = -parity;  // the mirror across a face normal to the component
+    const long long f = code >> 1;
     valid = vb[f] > .5f;
     return parity * (forward ? D.fwd[f] : m.A[D.N + f]);
+  }
+  // The donor-table entry of in-bounds face (q, axis): kDonorWall where exactly one side is solid;
+  // where both are, the reflect_voxel_donor mirror (2 f' + 1 when its parity is -1) or kDonorNone;
+  // else the face itself (2 f).
+  DI int donor_code(I3 q, int axis) const {
+    const Grid& g = m.g;
+    const bool left = g.solid(ax(q, axis, -1)), right = g.solid(q);
+    if (left != right) return kDonorWall;
+    if (!left) return (int)(2 * g.face_local(q, axis));
+    float reflection;
+    if (!reflect(q, axis, reflection)) return kDonorNone;
+    return (int)(2 * g.face_local(q, axis)) + (reflection < 0.f ? 1 : 0);
   }
   // sampled_component (coupled_motion.glslinc:112-137).  Fast path: when the donor block's corner
   // lo is inside the domain and no solid cell lies in the 3x3 (x, y) window around it, every
@@ -506,6 +517,18 @@ struct Mac {
     return true;
   }
 };
+
+// The donor table of every face (static geometry), built once at set-up.
+__global__ void __launch_bounds__(NT) k_mac_donor_table(const __grid_constant__ Dev D) {
+  const long long f = (long long)blockIdx.x * NT + threadIdx.x;
+  if (f >= D.NF) return;
+  Motion m(D);
+  Mac mc(m);
+  I3 q;
+  int axis;
+  m.g.unpack_face(f, q, axis);
+  D.mac_dtab[f] = mc.donor_code(q, axis);
+}
 
 // ---------------------------------------------------------------- op 27 / op 28
 // Face position of face (q, axis) in local coordinates (coupled_motion.glslinc:411).
@@ -833,6 +856,7 @@ int mac_blocks() {
     return 0;
   return sms * (per_sm > 0 ? per_sm : 1);
 }
+void launch_mac_donor_table(const Dev& D, cudaStream_t s) { k_mac_donor_table<<<grid_for(D.NF), NT, 0, s>>>(D); }
 void launch_maccormack(const Dev& D, cudaStream_t s) {
   pdl_launch(k_mac_reset, 1, 32, 0, s, D);
   pdl_launch(k_mac_list, grid_for(D.NF), NT, 0, s, D);

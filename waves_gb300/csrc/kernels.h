@@ -89,6 +89,7 @@ void launch_empty(cudaStream_t s);  // one empty one-thread kernel (probe calibr
 // k_motion.cu
 void launch_motion_cfl(const Dev& D, cudaStream_t s);
 void launch_sweep(const Dev& D, cudaStream_t s);
+void launch_mac_donor_table(const Dev& D, cudaStream_t s);  // static, once at set-up
 void launch_maccormack(const Dev& D, cudaStream_t s);
 int mac_blocks();   // resident blocks of the persistent MacCormack kernel (3 per SM form)
 int mac_blocks2();  // the same for the 2-per-SM form

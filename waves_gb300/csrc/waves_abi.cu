@@ -395,6 +395,11 @@ waves_status setup_device(waves_handle* h) {
   AL(D.mac_list, NF, false, "mac_list");
   AL(D.mac_ctr, wg::kMacCounters, false, "mac_counters");
   AL(D.mac_ovf, NF, false, "mac_handover");
+  if (NF >= (1LL << 30)) {  // donor-table entries hold 2 f + 1 in an int
+    h->err = "too many faces for the MacCormack donor table";
+    return WAVES_INVALID_ARG;
+  }
+  AL(D.mac_dtab, NF, false, "mac_donor_table");
   AL(D.geo_queue, N, false, "geometry_search_queue");
   AL(D.geo_qcount, 1, false, "geometry_search_count");
   {
@@ -1026,6 +1031,7 @@ waves_status waves_create(const waves_config* cfg, waves_handle** out) {
   if ((st = setup_device(h)) != WAVES_OK) return fail(st);
   wg::launch_mg_cols(h->D, h->stream);
   wg::launch_ext_masks(h->D, h->stream);
+  wg::launch_mac_donor_table(h->D, h->stream);
   wg::launch_initial(h->D, h->stream, h->probes);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     h->err = "initial commands failed";
