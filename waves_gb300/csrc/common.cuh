@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "dev.h"
+#include "exact_product.h"
 
 namespace wg {
 

@@ -880,6 +880,8 @@ template <class T, int RRB = RR> DI float row_sum(const MG& m, int l, int src, i
   if (!m.active<T>(l, i)) return ld_val(m.field<T>(src, l)[i]);
   const int S = m.D.lv[l].stencil;
   float sum = 0.f;
+  // unrolled so that the shared-memory loads run ahead of the additions (which stay in order)
+#pragma unroll 8
   for (int k = 0; k < S; k++) sum += prod[k * RRB + threadIdx.x];
   return sum;
 }
@@ -1061,10 +1063,10 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
       if (phase == 0) D.d[c.i] = z;
       // FP64 terms only where they can be other than zero
       if (rr != 0.f || !isfinite(z)) {
-        v[0] = (double)rr * (double)z;
-        v[1] = (double)rr * (double)rr;
+        v[0] = exact_product(rr, z);
+        v[1] = exact_product(rr, rr);
       }
-      if (bb != 0.f) v[2] = (double)bb * (double)bb;
+      if (bb != 0.f) v[2] = exact_product(bb, bb);
       vmax[0] = fabsf(rr);
     }
   }
@@ -1487,6 +1489,7 @@ __global__ void __launch_bounds__(kLegThreads, 1) k_mg_leg(const __grid_constant
           if (!m.active<T>(l, i)) ax = ld_val(x[i]);
           else {
             float sum = 0.f;
+#pragma unroll 8
             for (int k = 0; k < S; k++) sum += prod[k * cnt + r];
             ax = sum;
           }
@@ -1543,10 +1546,10 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_finish(const __gri
     D.z[i] = z;
     if (phase == 0) D.d[i] = z;
     if (r != 0.f || !isfinite(z)) {
-      v[0] = (double)r * (double)z;
-      v[1] = (double)r * (double)r;
+      v[0] = exact_product(r, z);
+      v[1] = exact_product(r, r);
     }
-    if (b != 0.f) v[2] = (double)b * (double)b;
+    if (b != 0.f) v[2] = exact_product(b, b);
     vmax[0] = fabsf(r);
   }
   const int ops[3] = {0, 0, 0};

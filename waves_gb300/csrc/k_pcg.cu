@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(NT) k_warm_decide(const __grid_constant__ Dev 
   if (i < D.N && D.kind[i] > 0) {
     I3 q = g.coord(i);
     const float rp = D.b[i] - operator_at(D, g, q, i, p), rn = D.b[i] - operator_at(D, g, q, i, D.net_p);
-    v[0] = (double)rp * (double)rp;
-    v[1] = (double)rn * (double)rn;
+    v[0] = exact_product(rp, rp);
+    v[1] = exact_product(rn, rn);
   }
   const int ops[2] = {0, 0};
   double out[2];
@@ -120,10 +120,10 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
     D.b[i] = bv;
     // FP64 terms only where they can be other than zero
     if (r != 0.f || !isfinite(z)) {
-      v[0] = (double)r * (double)z;
-      v[1] = (double)r * (double)r;
+      v[0] = exact_product(r, z);
+      v[1] = exact_product(r, r);
     }
-    if (bv != 0.f) v[2] = (double)bv * (double)bv;
+    if (bv != 0.f) v[2] = exact_product(bv, bv);
     vmax[0] = fabsf(r);
   }
   const int ops[3] = {0, 0, 0};
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D)
   if (i < D.N) {
     float qv = D.kind[i] > 0 ? operator_at(D, g, g.coord(i), i, D.d) : 0.f;
     D.q[i] = qv;
-    if (qv != 0.f) v[0] = (double)D.d[i] * (double)qv;  // dry cells add nothing
+    if (qv != 0.f) v[0] = exact_product(D.d[i], qv);  // dry cells add nothing
   }
   const int ops[1] = {0};
   double out[1];
