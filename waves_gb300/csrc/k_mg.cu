@@ -1109,7 +1109,9 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
 
 // Generic levels (l >= 1): one thread per cell.
 constexpr int kWideStencil = 40;
-template <class T, int NTB = NT>
+// RESTRICT: the instance for the restriction ops 3 and 5 (its unrolled child loads need more
+// registers than the sweeps and the prolongation, which run in the other instance).
+template <class T, int NTB = NT, bool RESTRICT = false>
 __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
@@ -1134,12 +1136,17 @@ __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int 
       if (l >= 1 && D.lv[l].stencil <= kWideStencil) return m.apply_wide<T, kWideStencil>(l, a, i, lin_s);
     return m.apply<T>(l, a, i, lin_s);
   };
+  if constexpr (!RESTRICT) {
+    switch (op) {
+      case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : ax()); break;
+      case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : ax()); break;
+      case 2: residual_update<T>(m, l, i, ax()); break;
+      case 4: prolong_cell<T>(m, l, a, b, i); break;
+    }
+    return;
+  }
   switch (op) {
-    case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : ax()); break;
-    case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : ax()); break;
-    case 2: residual_update<T>(m, l, i, ax()); break;
     case 3: restrict_cell<T>(m, l, i); break;
-    case 4: prolong_cell<T>(m, l, a, b, i); break;
     case 5:
       // restriction into level l fused with the level's first pre-smoothing sweep, which starts
       // from a zero iterate and so needs only the row's own b and scale (Chebyshev k = 1 into
@@ -1737,7 +1744,7 @@ template <class T> struct Cycle {
     int field = smooth(l, 1, true, false);
     if (l == 0) pdl_launch((k_mg0_residual<T>), grid0(), NT, 0, s, D, phase, field);
     else level_op(l, 2, field, 0, 0);
-    pdl_launch((k_mgl<T>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, restrict_fused(l + 1) ? 5 : 3, l + 1, 0, 0, 0);
+    pdl_launch((k_mgl<T, NT, true>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, restrict_fused(l + 1) ? 5 : 3, l + 1, 0, 0, 0);
     int cf = level(l + 1);
     pdl_launch((k_mgl<T>), gr, NT, 0, s, D, phase, 4, l, field, cf, 0);
     return smooth(l, field, false, l == 0 && D.mg_smoother == 1);

@@ -11,22 +11,31 @@ constexpr int NT = 256;
 
 // Fine 7-point operator applied to a vector that is zero off the wet set
 // (pressure_core.glslinc:119-125).
+// Every load (the six neighbours' kinds and values, the six coefficients) is issued before the
+// first test: a neighbour outside the domain loads from i instead and counts as 0, as before.
 DI float operator_at(const Dev& D, const Grid& g, I3 q, long long i, const float* x) {
-  float here = D.kind[i] > 0 ? x[i] : 0.f;
+  long long nb_i[6];
+  bool in[6];
+#pragma unroll
+  for (int face = 0; face < 6; face++) {
+    const I3 nb = g.wrap_cell(ax(q, face >> 1, (face & 1) ? 1 : -1));
+    in[face] = !g.outside(nb);
+    nb_i[face] = in[face] ? g.index3(nb) : i;
+  }
+  float kd[6], xv[6], kf[6];
+#pragma unroll
+  for (int face = 0; face < 6; face++) {
+    kd[face] = D.kind[nb_i[face]];
+    xv[face] = x[nb_i[face]];
+    kf[face] = D.coef[(long long)face * D.N + i];
+  }
+  const float here = D.kind[i] > 0 ? x[i] : 0.f;
   float result = 0.f;
-  int face = 0;
-  for (int axis = 0; axis < 3; axis++)
-    for (int sign = -1; sign <= 1; sign += 2) {
-      I3 nb = g.wrap_cell(ax(q, axis, sign));
-      float other = 0.f;
-      if (!g.outside(nb)) {
-        long long j = g.index3(nb);
-        if (D.kind[j] > 0) other = x[j];
-      }
-      float k = D.coef[(long long)face * D.N + i];
-      result += k * (here - other);
-      face++;
-    }
+#pragma unroll
+  for (int face = 0; face < 6; face++) {
+    const float other = (in[face] && kd[face] > 0) ? xv[face] : 0.f;
+    result += kf[face] * (here - other);
+  }
   return result;
 }
 
