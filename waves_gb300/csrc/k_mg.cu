@@ -1107,10 +1107,88 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg0_load(const __grid
   }
 }
 
+// Restriction into level l (op 3, or op 5 with the level's first pre-smoothing sweep) with four
+// lanes per coarse cell, used where the parent level's transfer is not an aggregation and coarsens
+// z (a children box of several planes; with one plane the extra lanes cost more than they
+// bring: 13.9 -> 38.8 us from level 0 on the beach): the (tz, ty) rows of
+// the children box (at most 4 x 4 rows of 4) are shared out, p = tz * ext_y + ty to lane p % 4, each
+// lane loading its rows' activity flags and residuals and forming their weighted terms; lane 0 then
+// adds every term in the (tz, ty, tx) order of restrict_cell, taking each from its lane with a
+// shuffle, and writes the cell as restrict_cell (and op 5's sweep) does.  The sums are the same
+// float operations in the same order; the lanes only load in parallel.  An aggregated parent
+// level (at most 2 x 2 x 2 children) is left to lane 0 with restrict_cell.
+template <class T>
+__global__ void __launch_bounds__(NT) k_mg_restrict4(const __grid_constant__ Dev D, int phase, int op, int l) {
+  grid_dep_wait(D.pdl_early);
+  if (!phase_on(D, phase)) return;
+  const MG m(D);
+  const int t = blockIdx.x * NT + threadIdx.x;
+  const int i = t >> 2, g = t & 3, lane = threadIdx.x & 31;
+  const MGLevelDev& cv = D.lv[l];
+  const MGLevelDev& pv = D.lv[l - 1];
+  const bool ok = i < cv.count;  // no lane leaves before the shuffles
+  const int ic = ok ? i : 0;
+  if (pv.aggregate) {  // the same for every thread of the launch
+    if (ok && g == 0) {
+      restrict_cell<T>(m, l, ic);
+      if (op == 5 && m.active<T>(l, ic)) {
+        if (D.mg_smoother == 1) cheb_update<T>(m, l, 1, 1, ic, true, 0.f);
+        else jacobi_update<T>(m, l, 1, 1, ic, 0.f);
+      }
+    }
+    return;
+  }
+  const T* r6 = m.field<T>(6, l - 1);
+  const I3 qc = m.coord(l, ic);
+  const bool act = ok && m.active<T>(l, ic);
+  const int* ix = D.rt_idx + cv.roff[0] + 4 * qc.x;
+  const int* iy = D.rt_idx + cv.roff[1] + 4 * qc.y;
+  const int* iz = D.rt_idx + cv.roff[2] + 4 * qc.z;
+  const float* wx = D.rt_w + cv.roff[0] + 4 * qc.x;
+  const float* wy = D.rt_w + cv.roff[1] + 4 * qc.y;
+  const float* wz = D.rt_w + cv.roff[2] + 4 * qc.z;
+  const int ey = cv.rext[1], P = cv.rext[2] * ey;
+  float term[4][4];
+  unsigned use = 0u;  // bit 4 jp + tx
+#pragma unroll
+  for (int jp = 0; jp < 4; jp++) {
+    const int p = g + 4 * jp, tz = p / ey, ty = p - tz * ey;
+#pragma unroll
+    for (int tx = 0; tx < 4; tx++) {
+      const bool in = act && p < P && tx < cv.rext[0] && iy[ty] >= 0 && ix[tx] >= 0;
+      const int j = in ? ix[tx] + pv.nx * (iy[ty] + pv.ny * iz[tz]) : 0;
+      const bool a = in && m.active<T>(l - 1, j);
+      const float r = ld_val(r6[j]);
+      term[jp][tx] = in ? (1.f * wx[tx] * wy[ty] * wz[tz]) * r : 0.f;
+      if (a) use |= 1u << (4 * jp + tx);
+    }
+  }
+  const int base = lane & ~3;
+  float sum = 0.f;
+#pragma unroll
+  for (int p = 0; p < 16; p++) {
+    const unsigned u = __shfl_sync(0xffffffffu, use, base + (p & 3));
+#pragma unroll
+    for (int tx = 0; tx < 4; tx++) {
+      const float v = __shfl_sync(0xffffffffu, term[p >> 2][tx], base + (p & 3));
+      if (p < P && ((u >> (4 * (p >> 2) + tx)) & 1u)) sum += v;
+    }
+  }
+  if (!ok || g != 0) return;
+  m.field<T>(0, l)[ic] = st_val<T>(sum);
+  m.field<T>(1, l)[ic] = st_val<T>(0.f);
+  m.field<T>(2, l)[ic] = st_val<T>(0.f);
+  if (op == 5 && act) {
+    if (D.mg_smoother == 1) cheb_update<T>(m, l, 1, 1, ic, true, 0.f);
+    else jacobi_update<T>(m, l, 1, 1, ic, 0.f);
+  }
+}
+
 // Generic levels (l >= 1): one thread per cell.
 constexpr int kWideStencil = 40;
-// RESTRICT: the instance for the restriction ops 3 and 5 (its unrolled child loads need more
-// registers than the sweeps and the prolongation, which run in the other instance).
+// RESTRICT: the instance for the restriction ops 3 and 5 where k_mg_restrict4 does not take them
+// (its unrolled child loads need more registers than the sweeps and the prolongation, which run
+// in the other instance).
 template <class T, int NTB = NT, bool RESTRICT = false>
 __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
   grid_dep_wait(D.pdl_early);
@@ -1744,7 +1822,15 @@ template <class T> struct Cycle {
     int field = smooth(l, 1, true, false);
     if (l == 0) pdl_launch((k_mg0_residual<T>), grid0(), NT, 0, s, D, phase, field);
     else level_op(l, 2, field, 0, 0);
-    pdl_launch((k_mgl<T, NT, true>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, restrict_fused(l + 1) ? 5 : 3, l + 1, 0, 0, 0);
+    {
+      // four lanes per coarse cell where the children box has several planes (a transfer that
+      // coarsens z: up to 16 rows of children); one thread per coarse cell otherwise
+      const int rop = restrict_fused(l + 1) ? 5 : 3;
+      if (!D.lv[l].aggregate && D.lv[l + 1].rext[2] > 1)
+        pdl_launch((k_mg_restrict4<T>), grid_for(4LL * D.lv[l + 1].count), NT, 0, s, D, phase, rop, l + 1);
+      else
+        pdl_launch((k_mgl<T, NT, true>), grid_for(D.lv[l + 1].count), NT, 0, s, D, phase, rop, l + 1, 0, 0, 0);
+    }
     int cf = level(l + 1);
     pdl_launch((k_mgl<T>), gr, NT, 0, s, D, phase, 4, l, field, cf, 0);
     return smooth(l, field, false, l == 0 && D.mg_smoother == 1);
