@@ -284,8 +284,10 @@ struct Coast {
     }
     surface(g.center(mk(x, 0, 0)).x, time, s0, s1);
   }
-  // velocity_c() at the position of face (q, axis); z does not enter the wave target
-  DI float velocity_face(const Grid& g, I3 q, int axis, float time) const {
+  // velocity_c() at the position of face (q, axis); z does not enter the wave target.  Not inlined
+  // (nor plane, fraction): most kernels call these only for the ghost columns left of the domain,
+  // and inlined copies of the wave target's arithmetic made their code several times larger.
+  __device__ __noinline__ float velocity_face(const Grid& g, I3 q, int axis, float time) const {
     if (axis == 2) return 0.f;
     const int j = q.x - D.wt_x0;
     int sl;
@@ -300,14 +302,14 @@ struct Coast {
     const F3 p = axis < 0 ? g.center(q) : face_position(g, q, axis);
     return 1.f - texp(-rate(p.x) * dt);
   }
-  DI float4 plane(const Grid& g, I3 q, float time) const {
+  __device__ __noinline__ float4 plane(const Grid& g, I3 q, float time) const {
     float s0, s1;
     F3 cq = g.center(q);
     surface_col(g, q.x, time, s0, s1);
     F3 normal = mf(-s1 * D.hx, D.hy, 0.f);
     return make_float4(normal.x, normal.y, normal.z, half_dot(normal) + s0 - cq.y);
   }
-  DI float fraction(const Grid& g, I3 q, float time) const {
+  __device__ __noinline__ float fraction(const Grid& g, I3 q, float time) const {
     float4 eq = plane(g, q, time);
     return clampf_(cube_volume(mf(eq.x, eq.y, eq.z), eq.w), 0.f, 1.f);
   }
