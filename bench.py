@@ -154,10 +154,12 @@ class Window:
             if st != 0:
                 raise RuntimeError(f"solver stopped with status {st} before t = {t_start}")
 
-    def measure(self, steps, warmup, barrier=None, clocks=None):
+    def measure(self, steps, warmup, barrier=None, clocks=None, checkpoint=False):
         s = self.s
         for _ in range(max(warmup, 3)):
             self.one_step()
+        # the state the timed steps start from (the end-to-end run replays the same span)
+        self.start_state = s.save() if checkpoint else None
         self.timing(True)
         c0, stats0 = s.control(), s.stats()
         if barrier:
@@ -239,7 +241,7 @@ def run_ours(args, world, rank, local):
         arm.s.load(checkpoint)
     s, lib, h = arm.s, arm.s.lib, arm.s.h
     with Clocks(local) as clk:
-        res = arm.measure(args.steps, args.warmup, barrier)
+        res = arm.measure(args.steps, args.warmup, barrier, checkpoint=args.e2e_frames != 0)
     c1 = res["c1"]
     # Roofline of the dominant kernel: one further step, host-scheduled, with every launch of the
     # probed kernels bracketed by CUDA events on the solver's stream (outside the timed region).
@@ -257,15 +259,17 @@ def run_ours(args, world, rank, local):
     out.update({"defect_rounds": rounds - active, "launches": launches, "clocks": clk.summary(), "t_end": c1[1],
                 "probes": probes if probe_trials else [], "plan": wg.mg_plan(arm.s.cfg)})
     # e2e: frames through the public API with host buffers, over the timed steps' simulated span,
-    # from the state the solver is in now (the waves' window continues)
+    # from the state the timed steps started from (restored from the checkpoint taken there)
     e2e = None
     if args.e2e_frames != 0:
+        s.load(arm.start_state)
         frames = args.e2e_frames if args.e2e_frames > 0 else max(1, int(round(res["sim_s"] * 60.0)))
         # page-locked host buffers for the per-frame surface export, as a renderer that reads the
         # surface every frame would hold them
         planes = torch.empty(4 * s.N, dtype=torch.float32, pin_memory=True).numpy()
         kinds = torch.empty(s.N, dtype=torch.float32, pin_memory=True).numpy()
         t_sim0 = s.control()[1]
+        arm.timing(True)
         w0 = time.perf_counter()
         for f in range(frames):
             s.request_time(t_sim0 + (f + 1) / 60.0)
@@ -273,9 +277,11 @@ def run_ours(args, world, rank, local):
             s.stats()
             lib.waves_export_surface(h, planes.ctypes.data_as(C.POINTER(C.c_float)), kinds.ctypes.data_as(C.POINTER(C.c_float)))
         w = time.perf_counter() - w0
+        e_motion, e_pressure, e_trials = arm.timing(True)
         sim_e = s.control()[1] - t_sim0
         e2e = {"sim_s": sim_e, "wall_s": w, "frames": frames, "window_s": [t_sim0, s.control()[1]],
-               "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8)}
+               "h2d": 8, "d2h": int(planes.nbytes + kinds.nbytes + 128 * 8),
+               "device_s": (e_motion + e_pressure) / 1e3, "trials": e_trials}
     out["e2e"] = e2e
     out["render"] = time_render(s, torch)
     arm.close()
@@ -528,7 +534,9 @@ def main():
         line["e2e"] = {"value": e2e_sim / max(e2e_wall, 1e-12), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                        "d2h_bytes_per_step": e["d2h"], "step": "one 1/60 s frame: request_time, run, stats, surface export",
                        "frames": e["frames"], "window_s": e["window_s"],
-                       "window": "the timed steps' simulated span again, continuing from where they ended"}
+                       "window": "the timed steps' simulated span again, from the state they started from (restored)",
+                       "device_sim_s_per_s": e["sim_s"] / e["device_s"] if e.get("device_s") else None,
+                       "trials": e.get("trials")}
     arms = dict(res["arms"])
     arms[("fp32" if args.mg == 32 else "bf16") + "_headline"] = summary(res)
     line["arms"] = arms
