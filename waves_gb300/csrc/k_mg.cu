@@ -1080,6 +1080,54 @@ __global__ void __launch_bounds__(NT) k_mg0_cheb(const __grid_constant__ Dev D, 
     else finalize_op9(D, out);
   }
 }
+// The last Chebyshev sweep of a V-cycle (k_mg0_cheb with fin >= 0) over two z planes per block:
+// each thread updates the cell of plane 2 bz and of plane 2 bz + 1, the same operations per cell,
+// and adds the two cells' FP64 terms before the block reduction, so the launch has half the
+// blocks, block trees and partials to combine.
+template <class T>
+__global__ void __launch_bounds__(NT) k_mg0_cheb_last(const __grid_constant__ Dev D, int phase, int source, float c1, float c2,
+                                                       int first_k, int src_zero) {
+  grid_dep_wait(D.pdl_early);
+  if (!phase_on(D, phase)) return;
+  double v[3] = {0, 0, 0};
+  float vmax[1] = {0.f};
+  for (int dz = 0; dz < 2; dz++) {
+    Cell0 c;
+    c.x = blockIdx.x * kTileX + (threadIdx.x & (kTileX - 1));
+    c.y = blockIdx.y * kTileY + threadIdx.x / kTileX;
+    c.z = 2 * blockIdx.z + dz;
+    c.ok = c.x < D.nx && c.y < D.ny && c.z < D.nz;
+    c.i = c.ok ? c.x + D.nx * (c.y + D.ny * c.z) : 0;
+    if (!c.ok) continue;
+    const T* __restrict__ x = field0<T>(D, source);
+    const T* v7 = field0<T>(D, 7);
+    const float b = ld_val(field0<T>(D, 0)[c.i]);
+    const float sc = ld_val(field0<T>(D, 4)[c.i]);
+    const float dprev = first_k ? 0.f : ld_val(v7[c.i]);
+    const float r = src_zero ? b : b - apply0<T>(D, x, c);
+    const float d = (first_k ? 0.f : c1 * dprev) + c2 * sc * r;
+    const float xv = (src_zero ? 0.f : ld_val(x[c.i])) + d;
+    const T xs = st_val<T>(xv);
+    const float rr = D.r[c.i], z = ld_val(xs), bb = D.b[c.i];
+    D.z[c.i] = z;
+    if (phase == 0) D.d[c.i] = z;
+    // FP64 terms only where they can be other than zero
+    if (rr != 0.f || !isfinite(z)) {
+      v[0] += exact_product(rr, z);
+      v[1] += exact_product(rr, rr);
+    }
+    if (bb != 0.f) v[2] += exact_product(bb, bb);
+    vmax[0] = mxf(vmax[0], fabsf(rr));
+  }
+  const int ops[3] = {0, 0, 0};
+  double out[4];
+  float fout[1];
+  if (last_block_reduce_mf<NT, 3, 1>(D, kSiteRZ, v, ops, vmax, out, fout) && threadIdx.x == 0) {
+    out[3] = (double)fout[0];
+    if (phase == 0) finalize_op4(D, out);
+    else finalize_op9(D, out);
+  }
+}
 template <class T> __global__ void __launch_bounds__(NT) k_mg0_residual(const __grid_constant__ Dev D, int phase, int f) {
   grid_dep_wait(D.pdl_early);
   if (!phase_on(D, phase)) return;
@@ -1763,8 +1811,12 @@ template <class T> struct Cycle {
       if (D.mg_smoother == 1) {
         if (l == 0)
           probed(kProbeSmooth0, s, smooth0_bytes(D, phase, sweep + 1, first ? 1 : 0, fin ? 1 : -1, sizeof(T)), [&] {
-            pdl_launch((k_mg0_cheb<T>), grid0(), NT, 0, s, D, phase, field, cheb_c1(sweep + 1), cheb_c2(sweep + 1), sweep == 0 ? 1 : 0,
-                                                 first ? 1 : 0, fin ? 1 : -1);
+            if (fin)
+              pdl_launch((k_mg0_cheb_last<T>), dim3(grid0().x, grid0().y, (unsigned)((D.nz + 1) / 2)), NT, 0, s, D, phase, field,
+                         cheb_c1(sweep + 1), cheb_c2(sweep + 1), sweep == 0 ? 1 : 0, first ? 1 : 0);
+            else
+              pdl_launch((k_mg0_cheb<T>), grid0(), NT, 0, s, D, phase, field, cheb_c1(sweep + 1), cheb_c2(sweep + 1),
+                         sweep == 0 ? 1 : 0, first ? 1 : 0, -1);
           });
         else level_op(l, 0, field, sweep + 1, first ? 1 : 0);
       } else if (l == 0)
