@@ -146,16 +146,19 @@ __global__ void __launch_bounds__(NT) k_cg_init(const __grid_constant__ Dev D) {
 }
 
 // ---------------------------------------------------------------- op 5 + 6 + 7
+// Two cells per thread (i and i + NT of the block's 2 NT cells): half the blocks, FP64 block trees
+// and partials of the dot product.
 __global__ void __launch_bounds__(NT) k_cg_matvec(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!solving(D)) return;
   Grid g(D);
-  long long i = (long long)blockIdx.x * NT + threadIdx.x;
   double v[1] = {0};
-  if (i < D.N) {
-    float qv = D.kind[i] > 0 ? operator_at(D, g, g.coord(i), i, D.d) : 0.f;
+  for (int h = 0; h < 2; h++) {
+    const long long i = (long long)blockIdx.x * (2 * NT) + h * NT + threadIdx.x;
+    if (i >= D.N) continue;
+    const float qv = D.kind[i] > 0 ? operator_at(D, g, g.coord(i), i, D.d) : 0.f;
     D.q[i] = qv;
-    if (qv != 0.f) v[0] = exact_product(D.d[i], qv);  // dry cells add nothing
+    if (qv != 0.f) v[0] += exact_product(D.d[i], qv);  // dry cells add nothing
   }
   const int ops[1] = {0};
   double out[1];
@@ -270,7 +273,7 @@ void launch_warm_start(const Dev& D, cudaStream_t s) {
   pdl_launch(k_warm_apply, grid_for(D.N), NT, 0, s, D);
 }
 void launch_cg_init(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_init, grid_for(D.N), NT, 0, s, D); }
-void launch_cg_matvec(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_matvec, grid_for(D.N), NT, 0, s, D); }
+void launch_cg_matvec(const Dev& D, cudaStream_t s) { pdl_launch(k_cg_matvec, grid_for((D.N + 1) / 2), NT, 0, s, D); }
 void launch_cg_update(const Dev& D, cudaStream_t s) {
   if (D.bf16) pdl_launch((k_cg_update<__nv_bfloat16>), grid_for(D.N), NT, 0, s, D);
   else pdl_launch((k_cg_update<float>), grid_for(D.N), NT, 0, s, D);
