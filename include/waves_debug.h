@@ -27,7 +27,7 @@ waves_status waves_debug_read(waves_handle* h, const char* name, void* out, size
  * no-op): per kind, the launches, their summed CUDA-event time on the handle's stream and their
  * summed algorithmic bytes (distinct inputs read once, outputs written once).  Kinds: 0 MacCormack
  * passes, 1 level-0 Chebyshev sweeps, 2 level >= 1 sweeps (product-parallel rows), 3 level >= 1
- * sweeps (one thread per row), 4 VOF flux + update, 5 every kernel of the trial (launches and
+ * sweeps of the large levels (four lanes per active row, or one thread per row), 4 VOF flux + update, 5 every kernel of the trial (launches and
  * time only), 6 and 7 the calibration after the trial: 64 launches of an empty kernel bracketed
  * the way a probed launch is (6 the outer, 7 the inner event pair), whose time per launch is the
  * cost the brackets add to each probed launch, 8 the coarse leg of the V-cycle in one cluster

@@ -72,16 +72,17 @@ def test_step_parity(gpu_lib, name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["beach_slope", "beach_slope_bf16"])
-@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_BOTTOM_GLOBAL=1", "WAVES_MG_COARSE=1",
-                                     "WAVES_MG_LEG=1"])
+@pytest.mark.parametrize("variant", ["WAVES_MG_ROWS_BELOW=0", "WAVES_MG_ROWS_BELOW=0,WAVES_MG_LANES=1",
+                                     "WAVES_MG_BOTTOM_GLOBAL=1", "WAVES_MG_COARSE=1", "WAVES_MG_LEG=1"])
 def test_step_parity_kernel_variants(gpu_lib, name, variant, monkeypatch):
-    """Kernel forms that the small grids above do not reach: the level >= 1 sweeps with one
-    thread per row (large levels use it; small ones use the product-parallel rows), the bottom
-    levels solved from global memory (used when they do not fit the shared-memory stage), the
-    coarse levels as one cooperative launch, and the coarse leg as one thread-block cluster
-    launch, instead of level by level."""
-    key, value = variant.split("=")
-    monkeypatch.setenv(key, value)
+    """Kernel forms that the small grids above do not reach: the level >= 1 sweeps of the large
+    levels (four lanes per active row, and with WAVES_MG_LANES=1 one thread per row; small levels
+    use the product-parallel rows), the bottom levels solved from global memory (used when they do
+    not fit the shared-memory stage), the coarse levels as one cooperative launch, and the coarse
+    leg as one thread-block cluster launch, instead of level by level."""
+    for setting in variant.split(","):
+        key, value = setting.split("=")
+        monkeypatch.setenv(key, value)
     cfg = CASES[name]()
     g = wg.WavesSolver(cfg)
     o = Oracle(cfg, 32)

@@ -208,7 +208,7 @@ class WavesKernelProbe(C.Structure):
 
 
 # Kinds of waves_debug_probe_trial (include/waves_debug.h): the kernel each probes.
-PROBE_KINDS = ["k_mac", "k_mg0_cheb", "k_mgl_rows", "k_mgl", "k_sweep_update", "all", "empty", "empty_inner", "k_mg_leg"]
+PROBE_KINDS = ["k_mac", "k_mg0_cheb", "k_mgl_rows", "k_mgl4", "k_sweep_update", "all", "empty", "empty_inner", "k_mg_leg"]
 
 
 # Every function declared in include/waves.h.

@@ -172,6 +172,7 @@ struct Dev {
   int mg_rows_below;         // levels with fewer rows use the product-parallel apply
   int mg_rows_rr;            // rows per block of the product-parallel apply (8, 16, 32 or 64)
   int mg_thread_nt;          // block size of the one-thread-per-row sweeps (128 or 256)
+  int mg_lanes;              // lanes per row of the large-level sweeps (4: k_mgl4, 1: k_mgl)
   int* mg_rowlist;           // active rows of each level >= 1 (level l at lv[l].off)
   unsigned* mg_rowcount;     // [kMaxLevels] entries of each list
   int mg_bottom_smem;        // bytes of the shared-memory bottom stage (0: bottom levels too large)

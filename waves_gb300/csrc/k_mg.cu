@@ -1286,6 +1286,76 @@ __global__ void __launch_bounds__(NTB) k_mgl(const __grid_constant__ Dev D, int 
   }
 }
 
+// Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a large level >= 1 whose stencil has
+// at most kWideStencil entries, with four lanes per active row: lane g loads the operator values and
+// neighbour values of the row's entries k = g, g + 4, g + 8, ... and forms their products; lane 0
+// then adds the products in stencil order k = 0..S-1, taking each from its lane with a shuffle, and
+// updates the row as k_mgl does.  Every product and every addition is the float operation that
+// MG::apply performs (the product rounded, then added, in the same order), so the bits are the
+// same; the lanes only load in parallel.  A level-1 sweep of the beach visits about 70,000 active
+// rows, which with one thread per row leaves about 14 warps per SM waiting on dependent loads.
+constexpr int kLaneEntries = kWideStencil / 4;
+template <class T>
+__global__ void __launch_bounds__(NT) k_mgl4(const __grid_constant__ Dev D, int phase, int op, int l, int a, int b, int c) {
+  grid_dep_wait(D.pdl_early);
+  if (!phase_on(D, phase)) return;
+  const MGLevelDev& lv = D.lv[l];
+  const int nrows = (int)D.mg_rowcount[l];
+  if ((int)((blockIdx.x * NT) >> 2) >= nrows) return;  // uniform over the block
+  __shared__ int lin[kWideStencil];
+  const int S = min(lv.stencil, kWideStencil);
+  for (int k = threadIdx.x; k < S; k += NT) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
+  __syncthreads();
+  const int t = blockIdx.x * NT + threadIdx.x;
+  if (((t & ~31) >> 2) >= nrows) return;  // the warp's first row: uniform over the warp
+  const int r = t >> 2, g = t & 3, lane = threadIdx.x & 31;
+  const bool ok = r < nrows;  // no lane of the warp leaves before the shuffles
+  const int i = D.mg_rowlist[lv.off + (ok ? r : nrows - 1)];
+  const MG m(D);
+  const bool need = !(op == 0 && c != 0) && !(op == 1 && b != 0);  // uniform over the launch
+  float ax = 0.f;
+  if (need) {
+    const T* x = m.field<T>(a, l);
+    const T* ell = (const T*)D.mgell + lv.eoff;
+    const int* col = D.mgcol + lv.eoff;
+    const I3 q = m.coord(l, i);
+    const bool inner = q.x >= 2 && q.x < lv.nx - 2 && q.y >= 2 && q.y < lv.ny - 2 && q.z >= 2 && q.z < lv.nz - 2;
+    float e[kLaneEntries], v[kLaneEntries];
+#pragma unroll
+    for (int j = 0; j < kLaneEntries; j++) {
+      const int k = 4 * j + g;
+      e[j] = 0.f;
+      v[j] = 0.f;
+      if (k < S) {
+        const long long at = (long long)k * lv.count + i;
+        const int n = inner ? i + lin[k] : __ldg(col + at);
+        e[j] = ld_val(ell[at]);
+        v[j] = ld_val(x[n]);
+      }
+    }
+    const bool act = m.active<T>(l, i);
+    const float here = ld_val(x[i]);
+    const int base = lane & ~3;
+    float sum = 0.f;
+#pragma unroll
+    for (int j = 0; j < kLaneEntries; j++) {
+      const float p = e[j] * v[j];
+#pragma unroll
+      for (int h = 0; h < 4; h++) {
+        const float term = __shfl_sync(0xffffffffu, p, base + h);
+        if (4 * j + h < S) sum += term;
+      }
+    }
+    ax = act ? sum : here;
+  }
+  if (!ok || g != 0) return;
+  switch (op) {
+    case 0: cheb_update<T>(m, l, a, b, i, c != 0, c != 0 ? 0.f : ax); break;
+    case 1: jacobi_update<T>(m, l, a, b, i, b ? 0.f : ax); break;
+    case 2: residual_update<T>(m, l, i, ax); break;
+  }
+}
+
 // Chebyshev (op 0), Jacobi (op 1) and residual (op 2) sweeps of a level >= 1 with the
 // product-parallel apply: RR rows per block.
 template <class T, int RRB = RR>
@@ -1792,7 +1862,9 @@ template <class T> struct Cycle {
       }, l);
     else
       probed(kProbeRowThread, s, bytes, [&] {
-        if (D.mg_thread_nt == 128)
+        if (D.mg_lanes == 4 && D.lv[l].stencil <= kWideStencil && op <= 2)
+          pdl_launch((k_mgl4<T>), (unsigned)((4LL * D.lv[l].count + NT - 1) / NT), NT, 0, s, D, phase, op, l, a, b, c);
+        else if (D.mg_thread_nt == 128)
           pdl_launch((k_mgl<T, 128>), (unsigned)((D.lv[l].count + 127) / 128), 128, 0, s, D, phase, op, l, a, b, c);
         else
           pdl_launch((k_mgl<T, NT>), grid_for(D.lv[l].count), NT, 0, s, D, phase, op, l, a, b, c);

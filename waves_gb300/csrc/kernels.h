@@ -18,7 +18,7 @@ enum ProbeKind {
   kProbeMac = 0,        // k_mac, MacCormack forward (op 27) and corrected (op 28) passes
   kProbeSmooth0 = 1,    // k_mg0_cheb, level-0 Chebyshev sweeps
   kProbeRows = 2,       // k_mgl_rows, level >= 1 sweeps with the product-parallel apply
-  kProbeRowThread = 3,  // k_mgl ops 0-2, level >= 1 sweeps with one thread per row
+  kProbeRowThread = 3,  // k_mgl4 (k_mgl with one lane per row) ops 0-2, level >= 1 sweeps of large levels
   kProbeSweepVof = 4,   // k_sweep_update, VOF flux + update of one direction
   kProbeAll = 5,        // every kernel of the trial (bytes not counted)
   kProbeEmpty = 6,      // calibration: an empty kernel bracketed as a probed launch is (kind + all)

@@ -608,6 +608,10 @@ waves_status setup_device(waves_handle* h) {
   // 14.52; 128-thread one-row-per-thread blocks 0.2 % faster than 256)
   D.mg_thread_nt = 128;
   if (const char* e = getenv("WAVES_MG_THREAD_NT")) D.mg_thread_nt = atoi(e) == 256 ? 256 : 128;
+  // four lanes per active row in the sweeps of the large levels (k_mgl4); WAVES_MG_LANES=1 keeps one
+  // thread per row (k_mgl).  Both give the same bits.
+  D.mg_lanes = 4;
+  if (const char* e = getenv("WAVES_MG_LANES")) D.mg_lanes = atoi(e) == 1 ? 1 : 4;
   D.mg_rows_rr = 16;
   if (const char* e = getenv("WAVES_MG_ROWS_RR")) {
     const int v = atoi(e);
