@@ -28,6 +28,18 @@ def test_python_symbol_list_matches_header():
     assert set(WAVES_ABI_SYMBOLS) == declared("waves.h")
 
 
+def test_probe_kind_names_match_the_library():
+    """One name per probe kind of the library (kernels.h numbers them up to kProbeCount), in the
+    order the debug header lists them."""
+    from waves_gb300.abi import PROBE_KINDS
+    text = open(os.path.join(ROOT, "waves_gb300", "csrc", "kernels.h")).read()
+    kinds = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(kProbe\w+)\s*=\s*(\d+)", text)}
+    assert kinds["kProbeCount"] == len(PROBE_KINDS)
+    assert PROBE_KINDS[kinds["kProbeRowThread"]] == "k_mgl4"
+    assert PROBE_KINDS[kinds["kProbeRows"]] == "k_mgl_rows"
+    assert PROBE_KINDS[kinds["kProbeLeg"]] == "k_mg_leg"
+
+
 def test_presets_without_gpu():
     lib = waves_gb300.load(build_if_missing=True)
     beach = waves_gb300.config("beach")

@@ -1937,10 +1937,9 @@ template <class T> struct Cycle {
         pdl_launch((k_mg_bottom_smem<T>), 1, 1024, D.mg_bottom_smem, s, D, phase, l);
       else
         pdl_launch((k_mg_bottom<T>), 1, 1024, 0, s, D, phase, l);
-      if (l == D.L - 1) {
-        if (D.lv[l].count <= 64) return 1;
-        return 1;  // 32 Jacobi sweeps end in field 1
-      }
+      // the bottom kernels leave the level's correction in field 1: the dense solve of the
+      // coarsest level, its 32 Jacobi sweeps where it has more than 64 rows, and the sub-cycle
+      // from mg_bottom down and back alike
       return bottom_field();
     }
     int field = smooth(l, 1, true, false);
