@@ -55,6 +55,7 @@ CASES = {
                                             stokes_second=1), 3),
     "beach_coarse": (beach_coarse, 2),
     "beach_slope": (beach_slope, 2),
+    "beach_coarse_jacobi_rebuild": (lambda: beach_coarse(mg_smoother=0, mg_smoothing=2, mg_maintenance=0), 2),
     "absorber": (lambda: beach_coarse(shape=6), 2),
 }
 
