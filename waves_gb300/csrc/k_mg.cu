@@ -452,28 +452,66 @@ template <class T> __global__ void __launch_bounds__(NT) k_mg_transfer(const __g
     D.mgtq[lv.toff + (long long)k * lv.count + i] = k < size ? MG::pack(m.coord(l + 1, ids[k])) : 0ull;
   }
 }
-// l1-Jacobi scale (pressure_multigrid.glslinc:183-189)
-template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(const __grid_constant__ Dev D, int l) {
+// l1-Jacobi scale (pressure_multigrid.glslinc:183-189) of level 0; the levels >= 1 take k_mg_scale8,
+// whose row sum runs over the level's stencil entries k = 0..S-1, adding |a_ij| for every entry
+// whose neighbour j does not repeat an earlier entry's.
+template <class T> __global__ void __launch_bounds__(NT) k_mg_scale(const __grid_constant__ Dev D) {
   grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
-  const MGLevelDev& lv = D.lv[l];
+  const int l = 0;
   int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= lv.count) return;
-  float sum = 0.f;
+  if (i >= D.lv[0].count) return;
   I3 q = m.coord(l, i);
-  if (l == 0) {
-    sum = m.fine_coef(12, i);
-    for (int axis = 0; axis < 3; axis++)
-      for (int side = 0; side < 2; side++)
-        if (m.active<T>(0, m.wrap(0, ax(q, axis, 2 * side - 1)))) sum += m.fine_coef(6 + 2 * axis + side, i);
-  } else {
-    for (int k = 0; k < lv.stencil; k++) {
-      I3 off = m.offset(l, k);
-      int j = m.wrap(l, addI(q, off));
-      if (m.unique_neighbor(l, i, off, j)) sum += fabsf(m.coefficient<T>(l, i, j));
+  float sum = m.fine_coef(12, i);
+  for (int axis = 0; axis < 3; axis++)
+    for (int side = 0; side < 2; side++)
+      if (m.active<T>(0, m.wrap(0, ax(q, axis, 2 * side - 1)))) sum += m.fine_coef(6 + 2 * axis + side, i);
+  if (!(sum > 0.f) || isnan(sum) || isinf(sum)) {
+    D.c[7] = 32;
+    return;
+  }
+  m.field<T>(4, l)[i] = st_val<T>(1.f / sum);
+}
+// The l1-Jacobi scale (pressure_multigrid.glslinc:183-189) of a level >= 1 with eight lanes per
+// row: lane g forms |a_ij| of the row's entries k = g, g + 8, g + 16, ... (-1 for an entry whose
+// neighbour repeats an earlier entry's, or past the stencil), and lane 0 adds the terms from the
+// eight lanes by shuffle in stencil order k = 0..S-1: the additions of the sequential loop over the
+// stencil, in its order, so the same bits, with the row's loads spread over eight lanes.
+constexpr int kScaleLanes = 8;
+template <class T> __global__ void __launch_bounds__(NT) k_mg_scale8(const __grid_constant__ Dev D, int l) {
+  grid_dep_wait(D.pdl_early);
+  if (!build_on(D) || D.hstate[8] == 0) return;
+  const MG m(D);
+  const MGLevelDev& lv = D.lv[l];
+  const int t = blockIdx.x * NT + threadIdx.x;
+  if ((t & ~31) / kScaleLanes >= lv.count) return;  // the warp's first row: uniform over the warp
+  const int r = t / kScaleLanes, g = t % kScaleLanes, lane = threadIdx.x & 31;
+  const bool ok = r < lv.count;  // no lane of the warp leaves before the shuffles
+  const int i = ok ? r : lv.count - 1;
+  const I3 q = m.coord(l, i);
+  constexpr int E = (kMaxStencil + kScaleLanes - 1) / kScaleLanes;
+  float term[E];
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int k = kScaleLanes * e + g;
+    term[e] = -1.f;
+    if (k < lv.stencil) {
+      const I3 off = m.offset(l, k);
+      const int j = m.wrap(l, addI(q, off));
+      if (m.unique_neighbor(l, i, off, j)) term[e] = fabsf(m.coefficient<T>(l, i, j));
     }
   }
+  const int base = lane & ~(kScaleLanes - 1);
+  float sum = 0.f;
+#pragma unroll
+  for (int e = 0; e < E; e++)
+#pragma unroll
+    for (int h = 0; h < kScaleLanes; h++) {
+      const float v = __shfl_sync(0xffffffffu, term[e], base + h);
+      if (!(v < 0.f)) sum += v;  // every |a_ij| (a NaN included), never the -1 of no term
+    }
+  if (!ok || g != 0) return;
   if (!(sum > 0.f) || isnan(sum) || isinf(sum)) {
     D.c[7] = 32;
     return;
@@ -756,22 +794,22 @@ template <class T> __global__ void __launch_bounds__(GP) k_mg_gal_pt(const __gri
   }
 }
 
-// ELL rows (pressure_multigrid.glslinc:176-182)
+// ELL rows (pressure_multigrid.glslinc:176-182), one thread per entry: entry k of row i (stored at
+// k * count + i) is the same function of (i, k) whichever thread forms it, and a row no longer
+// waits on its entries' loads one after the other (up to 125 of them on a coarse level).
 template <class T> __global__ void __launch_bounds__(NT) k_mg_ell(const __grid_constant__ Dev D, int l) {
   grid_dep_wait(D.pdl_early);
   if (!build_on(D) || D.hstate[8] == 0) return;
   MG m(D);
   const MGLevelDev& lv = D.lv[l];
-  int i = blockIdx.x * NT + threadIdx.x;
-  if (i >= lv.count) return;
-  I3 q = m.coord(l, i);
-  T* ell = (T*)D.mgell + lv.eoff;
-  for (int k = 0; k < lv.stencil; k++) {
-    I3 off = m.offset(l, k);
-    int j = m.wrap(l, addI(q, off));
-    float a = m.unique_neighbor(l, i, off, j) ? m.coefficient<T>(l, i, j) : 0.f;
-    ell[(long long)k * lv.count + i] = st_val<T>(a);
-  }
+  const long long t = (long long)blockIdx.x * NT + threadIdx.x;
+  if (t >= (long long)lv.stencil * lv.count) return;
+  const int k = (int)(t / lv.count), i = (int)(t - (long long)k * lv.count);
+  const I3 q = m.coord(l, i);
+  const I3 off = m.offset(l, k);
+  const int j = m.wrap(l, addI(q, off));
+  const float a = m.unique_neighbor(l, i, off, j) ? m.coefficient<T>(l, i, j) : 0.f;
+  ((T*)D.mgell + lv.eoff)[t] = st_val<T>(a);
 }
 // Dense Cholesky and L^-1 of the last level (pressure_mg_coarse.glslinc:34-48), one block.
 template <class T> __global__ void k_mg_chol(const __grid_constant__ Dev D, int l) {
@@ -2007,7 +2045,7 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
   for (int l = 1; l < D.L; l++) pdl_launch((k_mg_rowlist<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
   pdl_launch((k_mg_nb0<T>), grid_for(D.N), NT, 0, s, D);
   for (int l = 0; l + 1 < D.L; l++) pdl_launch((k_mg_transfer<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
-  pdl_launch((k_mg_scale<T>), grid_for(D.lv[0].count), NT, 0, s, D, 0);
+  pdl_launch((k_mg_scale<T>), grid_for(D.lv[0].count), NT, 0, s, D);
   for (int l = 1; l < D.L; l++) {
     int lo, ext[3];
     // the children box extents of fine level l-1 are the same for every coarse row
@@ -2029,9 +2067,9 @@ template <class T> void build(const Dev& D, cudaStream_t s) {
       const int slots = D.lv[l].gal_slots > 0 ? D.lv[l].gal_slots : 125;
       pdl_launch((k_mg_galerkin<T>), gr, GT, (size_t)slots * GT * sizeof(float), s, D, l - 1, ext[0], ext[1], ext[2]);
     }
-    pdl_launch((k_mg_scale<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+    pdl_launch((k_mg_scale8<T>), grid_for((long long)kScaleLanes * D.lv[l].count), NT, 0, s, D, l);
   }
-  for (int l = 1; l < D.L; l++) pdl_launch((k_mg_ell<T>), grid_for(D.lv[l].count), NT, 0, s, D, l);
+  for (int l = 1; l < D.L; l++) pdl_launch((k_mg_ell<T>), grid_for((long long)D.lv[l].stencil * D.lv[l].count), NT, 0, s, D, l);
   if (D.lv[D.L - 1].count <= 64) pdl_launch((k_mg_chol<T>), 1, 64, 0, s, D, D.L - 1);
   pdl_launch(k_hs_record, 1, 1, 0, s, D);
 }
