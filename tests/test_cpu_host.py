@@ -59,6 +59,16 @@ def test_bench_roofline_picks_the_largest_probed_time():
     assert roof["achieved"] == pytest.approx(100e6 / 492e-6 / 1e9)
 
 
+def test_bench_traffic_table_covers_the_probed_kernels():
+    """profiles/dram_traffic.txt gives a DRAM figure for every probed kernel the bench can report as
+    the dominant one, under the name the library's probe list uses."""
+    from waves_gb300.abi import PROBE_KINDS
+    traffic = load_bench().ncu_traffic()
+    for name in ("k_mac", "k_mg0_cheb", "k_mgl_rows", "k_mgl4", "k_sweep_update"):
+        assert name in PROBE_KINDS
+        assert traffic.get(name, 0.0) > 0.0, name
+
+
 def test_mg_plan_of_the_beach_and_the_large_grid():
     """waves_mg_plan (no device): the level plan of pressure_multigrid.gd:37-69 for the 310x48x80
     beach (x and y halved first, z kept at hz = 2 hx; aggregation from level 2) and the 620x96x160
