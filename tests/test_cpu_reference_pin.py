@@ -11,6 +11,7 @@ The configurations are the parity cases the reference can express: its push cons
 surface phase and its CFL number is 0.45.
 """
 import math
+import os
 
 import pytest
 
@@ -58,6 +59,20 @@ CASES = {
     "beach_coarse_jacobi_rebuild": (lambda: beach_coarse(mg_smoother=0, mg_smoothing=2, mg_maintenance=0), 2),
     "absorber": (lambda: beach_coarse(shape=6), 2),
 }
+
+
+@pytest.mark.skipif(os.environ.get("WAVES_LONG") != "1", reason="about 35 minutes of one core: set WAVES_LONG=1")
+def test_oracle_agrees_with_the_reference_shaders_on_the_full_beach():
+    """The metric's own grid, the 310x48x80 beach of lab_runner.gd:26 (the oracle's preset), over
+    its first two accepted steps, every dispatch unit, as the small cases below."""
+    ls = Lockstep(oracle_config("beach"))
+    ls.run_steps(2)
+    bad, report = ls.report()
+    totals = ls.totals()
+    print(f"beach 310x48x80: {totals}")
+    assert ls.control()[2] == 2
+    assert bad == 0, report
+    ls.close()
 
 
 @pytest.mark.parametrize("name", list(CASES))
