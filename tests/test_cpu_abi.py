@@ -50,6 +50,34 @@ def test_presets_without_gpu():
     assert abs(lib.waves_dispersion_k(1.4, 0.45) - 2.525) < 1e-3
 
 
+def test_create_rejects_invalid_configurations_before_touching_a_device():
+    """waves_create checks the configuration before it looks for a device: every invalid field
+    gives WAVES_INVALID_ARG (1) with no handle, here as on a GPU host; a valid one without a GPU
+    gives WAVES_NO_DEVICE (3), never a CPU fallback."""
+    import ctypes as C
+    lib = waves_gb300.load(build_if_missing=True)
+    bad = [("n", (1, 16, 8)), ("n", (16, 1, 8)), ("n", (16, 16, 0)), ("spacing", (0.0, 0.05, 0.05)),
+           ("spacing", (0.05, -0.05, 0.05)), ("spacing", (0.05, 0.05, float("nan"))), ("dt", 0.0),
+           ("mg_smoothing", 0), ("mg_smoothing", 9), ("mg_lag", 0), ("mg_precision", 8),
+           ("iterations_per_batch", 0)]
+    for field, value in bad:
+        cfg = waves_gb300.config("tank")
+        if isinstance(value, tuple):
+            for i, x in enumerate(value):
+                getattr(cfg, field)[i] = x
+        else:
+            setattr(cfg, field, value)
+        h = C.c_void_p(1)
+        assert lib.waves_create(C.byref(cfg), C.byref(h)) == 1, (field, value)
+        assert not h.value, (field, value)
+    assert lib.waves_create(None, C.byref(C.c_void_p())) == 1
+    import torch
+    if not torch.cuda.is_available():
+        h = C.c_void_p(1)
+        assert lib.waves_create(C.byref(waves_gb300.config("tank")), C.byref(h)) == 3
+        assert not h.value
+
+
 def test_create_without_device_fails_cleanly(monkeypatch):
     # No GPU in this container: waves_create must report an error, not crash or fall back.
     import torch
