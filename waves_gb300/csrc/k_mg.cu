@@ -1341,7 +1341,7 @@ __global__ void __launch_bounds__(NT) k_mgl4(const __grid_constant__ Dev D, int 
   const int nrows = (int)D.mg_rowcount[l];
   if ((int)((blockIdx.x * NT) >> 2) >= nrows) return;  // uniform over the block
   __shared__ int lin[kWideStencil];
-  const int S = min(lv.stencil, kWideStencil);
+  const int S = min(lv.stencil, kWideStencil);  // Cycle::level_op launches this only for S <= kWideStencil
   for (int k = threadIdx.x; k < S; k += NT) lin[k] = __ldg(D.stencil_lin + lv.soff + k);
   __syncthreads();
   const int t = blockIdx.x * NT + threadIdx.x;
