@@ -13,6 +13,7 @@ surface phase and its CFL number is 0.45.
 import math
 import os
 
+import numpy as np
 import pytest
 
 from tests.oracle_ref import oracle_config
@@ -108,3 +109,34 @@ def test_free_reference_and_oracle_accept_the_same_steps():
         differing += [(step, k, float(cr[k]), co[k]) for k in (8, 18, 58) if cr[k] != co[k]]
     print("differing (step, entry, reference, oracle):", differing)
     r.close()
+
+
+@pytest.mark.skipif(os.environ.get("WAVES_LONG") != "1", reason="about 15 minutes: set WAVES_LONG=1")
+def test_free_reference_and_oracle_over_two_seconds_of_the_coarse_beach():
+    """The free run against the oracle over the first 240 accepted steps (2 simulated seconds) of
+    the coarse beach: every step accepted on both sides with no rejection, retry or halt, at
+    accepted times that differ only by the FP32 accumulation of the reference's clock; the CG
+    iteration totals, the steps whose defect-correction flag differs and the largest bank
+    difference are printed."""
+    from tests.oracle_ref import Oracle
+    cfg = beach_coarse()
+    r, o = FreeReference(cfg), Oracle(cfg, 32)
+    iters_r = iters_o = 0
+    defect_steps, worst_dt, worst_bank = 0, 0.0, 0.0
+    for step in range(1, 241):
+        for s in (r, o):
+            s.request_steps(step)
+            s.run()
+        cr, co = r.control(), o.control()
+        assert cr[2] == co[2] == step and cr[3] == co[3] == 0 and cr[7] == co[7] == 0, step
+        worst_dt = max(worst_dt, abs(float(cr[1]) - co[1]))
+        iters_r += int(cr[8])
+        iters_o += int(co[8])
+        defect_steps += int(cr[58] != co[58])
+        worst_bank = max(worst_bank, float(np.max(np.abs(r.bank().astype(np.float64) - o.bank().astype(np.float64)))))
+    print(f"coarse beach, 240 steps to t = {co[1]:.4f} s: CG iterations reference {iters_r}, oracle {iters_o}; "
+          f"defect-correction flag differs in {defect_steps} steps; max |t - t_ref| {worst_dt:.2e} s; "
+          f"largest bank difference {worst_bank:.3g}")
+    assert worst_dt <= 1e-5
+    r.close()
+    o.close()
